@@ -1,0 +1,366 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 MHD timestep (Gcell-updates/s per RK substep).
+
+Default workload (N=1): isothermal compressible MHD, 7 fields, 1024^3
+periodic box L=2*pi, FP32 state with compensated 2N accumulation,
+nu=eta=5e-4, steady helical ABC forcing at k=2 with amplitude 0.02, uu=0,
+lnrho=0, aa Gaussian noise 1e-5 (seeded, generated on the device), fixed
+dt=2e-4.  A step is one full RK3 step (3 substep kernel launches).
+
+  value      whole-job Gcell-updates/s per substep, device-resident state,
+             CUDA events on the launching stream around exactly K steps;
+  e2e        the same metric through the reference plug-in C ABI
+             (initializeGPU/loadFarray, substepGPU x3 + getGPUReducedVars per
+             step, copyFarray) with pinned host buffers, copies inside the
+             timed region;
+  roofline   algorithmic HBM bytes per launch / mean launch duration of the
+             substep kernel against the measured copy bandwidth;
+  cpu_baseline  the FP64 oracle (C restatement of the reference Fortran) on
+             all host cores over a bounded sample.
+
+--impl reference runs that CPU implementation alone on the same metric.
+Under torchrun with N>1 every rank advances its own replica (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FALLBACK_HBM_GBS = 6800.0
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def bytes_per_cell_substep(nf: int, precision: int, comp: bool) -> float:
+    """Algorithmic HBM bytes per interior cell and substep.
+
+    FP32 compensated: read f, read df/carry, write df/carry, write f on every substep: 4*nf*4.
+    FP64 (and FP32 without compensation): substep 1 reads f, writes df and f (3 nf);
+    substep 2 reads f and df, writes both (4 nf); substep 3 reads f and df, writes f (3 nf,
+    df is dead after the last substep): mean 10/3 * nf * s."""
+    if precision == 4 and comp:
+        return 4.0 * nf * 4
+    return 10.0 / 3.0 * nf * precision
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def headline_params(pc, n: int, precision: int, lentropy: int = 0):
+    p = pc.default_params(nx=n, ny=n, nz=n, lentropy=lentropy, precision=precision, comp=1,
+                          gamma=1.0 if not lentropy else 5.0 / 3.0, nu=5e-4, eta=5e-4, chi=5e-4 if lentropy else 0.0,
+                          dt=2e-4, lforcing_cont=1, ampl_ff=0.02, kf=2.0, relhel=1.0)
+    return p
+
+
+def init_headline(box, p):
+    iax = 5 if p.lentropy else 4
+    for k in range(iax):
+        box.init_field(k, "zero")
+    for k in range(3):
+        box.init_field(iax + k, "zero")
+        box.init_field(iax + k, "noise", ampl=1e-5, seed=20260 + k)
+
+
+def time_box_steps(pc, torch, box, stream, steps: int) -> tuple[float, int]:
+    L = pc.load()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    n0 = L.pcgb_launch_count()
+    e0.record(stream)
+    box.steps(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), int(L.pcgb_launch_count() - n0)
+
+
+def cpu_oracle_rate(n: int, steps: int, threads: int, lentropy: int = 0) -> tuple[float, float, dict]:
+    """Gcell-updates/s per substep of the FP64 oracle on an n^3 sample of the headline physics."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    op = O.make_params(nx=n, ny=n, nz=n, lentropy=lentropy, gamma=1.0 if not lentropy else 5.0 / 3.0,
+                       nu=5e-4, eta=5e-4, chi=5e-4 if lentropy else 0.0, lforcing_cont=1, ampl_ff=0.02, kf=2.0)
+    f = O.empty_f(op)
+    df = O.empty_f(op)
+    rng = np.random.Generator(np.random.PCG64(1))
+    iax = 5 if lentropy else 4
+    f[3:-3, 3:-3, 3:-3, iax:iax + 3] = 1e-5 * rng.standard_normal((n, n, n, 3))
+    t, dt = 0.0, 2e-4
+    O.time_step(op, f, df, t, dt, False, nthreads=threads)   # warm-up (page-in, thread spin-up)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        t, dt, _ = O.time_step(op, f, df, t, dt, False, nthreads=threads)
+    el = time.perf_counter() - t0
+    return n ** 3 * 3 * steps / el / 1e9, el, {"n": n, "steps": steps}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    n = args.cpu_sample_n
+    per = []
+    for i in range(args.warmup + args.steps):
+        rate, el, _ = cpu_oracle_rate(n, 1, threads)
+        if i >= args.warmup:
+            per.append((rate, el))
+    total_cells = n ** 3 * 3 * len(per)
+    total_t = sum(e for _, e in per)
+    value = total_cells / total_t / 1e9
+    line = {
+        "impl": "reference", "metric": "Gcell-updates/s per RK substep", "value": value,
+        "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_t / len(per), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"isothermal MHD {args.n}^3 headline physics, CPU sample {n}^3 per step",
+                   "sample_n": n},
+        "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{n}^3 box, 1 RK3 step per timed step, FP64 oracle, OpenMP {threads} threads"},
+        "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_setup()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    pc = importlib.import_module("pencil-code_gb300")
+    gpu = importlib.import_module("pencil-code_gb300.gpu")
+    L = pc.load()
+    stream = torch.cuda.Stream()
+    L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
+
+    n, prec = args.n, args.precision
+    p = headline_params(pc, n, prec, args.lentropy)
+    if args.tile >= 0:
+        p.tile = args.tile
+    if args.zdepth > 0:
+        p.zdepth = args.zdepth
+    nf = 8 if args.lentropy else 7
+    box = pc.Box(p)
+    init_headline(box, p)
+    info = box.info()
+    box.steps(args.warmup)
+    box.sync()
+
+    sampler = ClockSampler(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    sampler.start()
+    ms, launches = time_box_steps(pc, torch, box, stream, args.steps)
+    clocks = sampler.stop()
+    box.sync()
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    cells = float(n) ** 3
+    value = ws * cells * 3 * args.steps / (ms / 1e3) / 1e9
+    per_launch_ms = ms / launches if launches else float("nan")
+    bpc = bytes_per_cell_substep(nf, prec, True)
+    achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tj = json.load(open(tpath))
+            key = f"f{8 * prec}_{nf}"
+            if key in tj:
+                traffic = tj[key]["bytes_per_cell_substep"] * cells
+        except Exception:
+            traffic = None
+    box.close()
+    del box
+
+    # ---- e2e through the plug-in C ABI with pinned host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, pc, gpu, torch, stream, p, nf)
+
+    # ---- CPU baseline (rank 0, N=1 only) ----
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, el, smp = cpu_oracle_rate(args.cpu_sample_n, args.cpu_sample_steps, threads, args.lentropy)
+        cpu = {"value": rate, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{smp['n']}^3 box, {smp['steps']} RK3 steps of the same physics, FP64 oracle "
+                         f"(C restatement of the reference Fortran), OpenMP {threads} threads, {el:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": "Gcell-updates/s per RK substep", "value": value, "unit": "Gcell-updates/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if prec == 4 else "f64", "data": "synthetic (seeded on device)",
+            "config": {"workload": f"{'entropy' if args.lentropy else 'isothermal'} MHD {n}^3, {nf} fields, "
+                                   f"{'FP32 compensated' if prec == 4 else 'FP64'}, nu=eta=5e-4, ABC k=2 ampl 0.02, "
+                                   f"dt=2e-4", "grid": n, "fields": nf,
+                       "tile": info["tile"], "zdepth": info["zdepth"],
+                       "l2": "inputs larger than L2 (state %.1f GB)" % (3 * nf * cells * prec / 1e9),
+                       "parallelism": f"replicas x{ws}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "bytes_per_cell_substep": bpc},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_e2e(args, pc, gpu, torch, stream, p, nf):
+    n = p.nx
+    shape = (n + 6, n + 6, n + 6, nf)
+    nbytes = int(np.prod(shape)) * 8
+    try:
+        avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    except Exception:
+        avail = 0
+    if avail and nbytes > 0.45 * avail:
+        return {"value": None, "unit": "Gcell-updates/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                "note": f"host f-array of {nbytes / 1e9:.1f} GB exceeds the host memory budget"}
+    ht = torch.zeros(int(np.prod(shape)), dtype=torch.float64, pin_memory=True)
+    fh = ht.numpy().reshape(shape, order="F")
+    iax = 5 if p.lentropy else 4
+    rng = np.random.Generator(np.random.PCG64(7))
+    for k in range(3):
+        fh[3:-3, 3:-3, 3:-3, iax + k] = 1e-5 * rng.standard_normal((n, n, n))
+    L = pc.load()
+    gpu.initialize_gpu(fh, p, t=0.0, nt=0)
+    red = np.zeros(gpu.n_gpu_reduced_vars)
+    rp = red.ctypes.data_as(C.POINTER(C.c_double))
+    # warm-up through the same calls
+    gpu.load_farray_to_gpu()
+    for _ in range(args.warmup):
+        for s in (1, 2, 3):
+            L.substepGPU(s, 0.0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gpu.load_farray_to_gpu()
+    for _ in range(args.steps):
+        for s in (1, 2, 3):
+            L.substepGPU(s, 0.0)
+        L.getGPUReducedVars(rp)
+    gpu.copy_farray_from_gpu(fh)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    rc, msg = pc.lib.last_error() if hasattr(pc, "lib") else (0, "")
+    gpu.finalize_gpu()
+    cells = float(n) ** 3
+    return {"value": cells * 3 * args.steps / el / 1e9, "unit": "Gcell-updates/s",
+            "h2d_bytes_per_step": nbytes / args.steps, "d2h_bytes_per_step": nbytes / args.steps + red.nbytes,
+            "what": "loadFarray + K x (substepGPU x3 + getGPUReducedVars) + copyFarray, pinned host f-array "
+                    "(REAL=double), wall clock"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--precision", type=int, default=4, choices=[4, 8])
+    ap.add_argument("--lentropy", type=int, default=0)
+    ap.add_argument("--tile", type=int, default=-1)
+    ap.add_argument("--zdepth", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sample-n", type=int, default=96)
+    ap.add_argument("--cpu-sample-steps", type=int, default=3)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

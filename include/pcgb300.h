@@ -1,0 +1,242 @@
+/*
+ * pcgb300.h -- C ABI of libpcgb300.so, the GB300-native replacement for the
+ * Pencil Code GPU plug-in (the library the Fortran module `GPU`,
+ * src/gpu_astaroth.f90, links through src/gpu_astaroth_ansi.c).
+ *
+ * Two groups of entry points:
+ *
+ *  1. The reference plug-in set, same names, argument meaning and void
+ *     returns as the C-linkage prototypes of src/gpu_astaroth_ansi.c:23-55
+ *     (implemented by src/astaroth/gpu_astaroth.cc in the reference), plus
+ *     the Fortran-callable FTNIZE wrappers of src/gpu_astaroth_ansi.c:72-289
+ *     (`name_`, gfortran convention, src/headers_c.h:30-37).  REAL is double
+ *     (the REAL_PRECISION=double build, src/headers_c.h:11-25); FINT is int.
+ *
+ *  2. Native extensions (prefix pcgb_): the parameter block that stands in for
+ *     the Fortran module variables the reference reads by address
+ *     (src/global_pushpars.f90:6-60, gpu_astaroth_ansi.c:59-61), error
+ *     reporting, and the box / batch / server API used for ensembles and
+ *     serving.
+ *
+ * Errors: the reference prints and exits (gpu_astaroth.cc:2074-2078).  Here
+ * every failure is recorded in a sticky code read by pcgb_last_error(); no
+ * call blocks without a bound.
+ */
+#ifndef PCGB300_H
+#define PCGB300_H
+
+#include <stddef.h>
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef double REAL_PCGB; /* REAL of the double build */
+
+/* ---------------------------------------------------------------------------
+ * Parameter block.  Field meanings follow the reference namelists:
+ *   &init_pars xyz0, Lxyz (param_io.f90:82), grid sizes (cparam.local),
+ *   &eos_init_pars gamma, cs0, rho0, cp (eos_idealgas.f90),
+ *   &viscosity_run_pars nu (ivisc='nu-const'), &magnetic_run_pars eta, b_ext,
+ *   &entropy_run_pars chi (iheatcond='chi-const'),
+ *   &forcing_run_pars iforcing_cont='ABC', ampl_ff, k1_ff, relhel,
+ *   &hydro_run_pars lforcing_cont_uu / ampl_fcont_uu,
+ *   &run_pars dt, cdt, cdtv (cdata.f90:235-239).
+ * ------------------------------------------------------------------------- */
+typedef struct pcgb_params {
+  int nx, ny, nz;          /* nxgrid, nygrid, nzgrid */
+  int lentropy;            /* 0: ENTROPY=noentropy (7 fields), 1: entropy (8 fields) */
+  int precision;           /* device state: 8 = FP64, 4 = FP32 */
+  int comp;                /* FP32 only: compensated 2N accumulation (1 = on) */
+  double xyz0[3], Lxyz[3];
+  double gamma, cs0, rho0, cp;
+  double nu, eta, chi, mu0;
+  int lforcing_cont;       /* continuous ABC forcing added to duu */
+  double ampl_ff, kf, relhel, abc_a, abc_b, abc_c, ampl_fcont_uu;
+  double b_ext[3];
+  int lohmic_heat, lviscosity_heat;
+  double cdt, cdtv;
+  double dt;               /* fixed dt; 0 selects the CFL timestep (ldt) */
+  int dt_mode;             /* with dt == 0: 1 = lagged (reference GPU default), 2 = current (CPU semantics) */
+  int diag_every;          /* device diagnostics every diag_every steps (0: on request only) */
+  int tile;                /* kernel tile variant, -1 = choose automatically */
+  int zdepth;              /* z-sweep depth, 0 = choose automatically */
+} pcgb_params;
+
+/* Defaults of the reference (cdata.f90:211,235,239; eos_idealgas.f90:47;
+   forcing.f90:37,129; hydro.f90:283; magnetic.f90:247; entropy.f90:139). */
+void pcgb_default_params(pcgb_params* p);
+
+/* Set the parameters used by initializeGPU / reloadConfig (stands in for the
+   Fortran module variables, src/global_pushpars.f90). Returns 0 or an error. */
+int pcgb_set_params(const pcgb_params* p);
+
+/* Sticky error code of the last failing call (0 = none) and its text. */
+int pcgb_last_error(void);
+const char* pcgb_error_string(int code);
+void pcgb_clear_error(void);
+
+/* Stream used for all device work (default: a library-owned stream).  Passing
+   a cudaStream_t lets a caller time the kernels with its own events. */
+void pcgb_set_stream(void* cuda_stream);
+void* pcgb_get_stream(void);
+
+/* ---------------------------------------------------------------------------
+ * 1. Reference plug-in entry points (src/gpu_astaroth_ansi.c:23-55).
+ * ------------------------------------------------------------------------- */
+
+/* gpu_astaroth_ansi.c:23 -- registration hook (allocations happen in initializeGPU). */
+void registerGPU(void);
+/* gpu_astaroth_ansi.c:24 -- bind the host f-array f(mx,my,mz,mvar) (Fortran
+   order, ghosts included), allocate device state for the parameter block set
+   by pcgb_set_params, and set time t.  comm is ignored (one GPU).
+   cpu_dt != 0 selects the CPU timestep semantics (lcpu_timestep_on_gpu,
+   gpu_astaroth.f90:19-23); autotune != 0 runs the tile autotuner. */
+void initializeGPU(REAL_PCGB* f, int comm, double t, int nt, int read_all, int cpu_dt, int autotune);
+/* gpu_astaroth_ansi.c:25 -- free all device state. */
+void finalizeGPU(void);
+/* gpu_astaroth_ansi.c:26 -- device pointer of the input f buffer (getFArrayIn). */
+void getFArrayIn(REAL_PCGB** p);
+/* gpu_astaroth_ansi.c:27 -- one full RK substep (RHS, 2N update, ghosts, dt on
+   substep 1), gpu_astaroth.cc:1672.  isubstep is 1-based and must follow the
+   device's own substep counter. */
+void substepGPU(int isubstep, double t);
+/* gpu_astaroth_ansi.c:28 -- nothing to do for this physics (gpu_astaroth.cc:1320). */
+void beforeBoundaryGPU(bool lrmv, int isubstep, double t, bool lsubstep);
+/* gpu_astaroth_ansi.c:29 -- nothing to do for this physics (gpu_astaroth.cc:1515). */
+void afterSubStepGPU(void);
+/* gpu_astaroth_ansi.c:30 -- no radiative transfer on this path. */
+void radTransfer(void);
+/* gpu_astaroth_ansi.c:31 -- copy the device f (mvar fields, ghosts included)
+   into the host array f (gpu_astaroth.cc:1719). */
+void copyFarray(REAL_PCGB* f);
+/* gpu_astaroth_ansi.c:32 -- copy the bound host f-array to the device and
+   refresh periodic ghosts (gpu_astaroth.cc:1947). */
+void loadFarray(void);
+/* gpu_astaroth_ansi.c:33 -- re-read the parameter block into device state. */
+void reloadConfig(void);
+/* gpu_astaroth_ansi.c:34-39 -- parameter updates by index or name.  Index
+   order is the field order of pcgb_params' double members starting at xyz0;
+   names are the pcgb_params member names.  *Name variants return 0 on
+   success and -1 for an unknown name. */
+void updateInConfigArr(int index);
+int updateInConfigArrName(char* name);
+void updateInConfigScal(int index, REAL_PCGB value);
+int updateInConfigScalName(char* name, REAL_PCGB value);
+void updateInConfigVec(int index, REAL_PCGB* value);
+int updateInConfigVecName(char* name, REAL_PCGB* value);
+/* gpu_astaroth_ansi.c:40 -- compute the first timestep if none is known
+   (GpuCalcDt, gpu_astaroth.cc:546). */
+void prepareForFirstSubstep(double t);
+/* gpu_astaroth_ansi.c:41 -- not provided by the reference either. */
+void random_initial_condition(void);
+/* gpu_astaroth_ansi.c:42 -- reduced diagnostics of the last diagnostic step:
+   dst[0..11] = urms, umax, brms, bmax, ekin, rhom, divbrms, jrms, abm, dt, t,
+   step.  (The reference returns module-specific sums, gpu_astaroth.cc:2486.) */
+void getGPUReducedVars(REAL_PCGB* dst);
+/* gpu_astaroth_ansi.c:43 -- compare device ghost cells with a periodic fill
+   of the device interior; prints the maximum difference (gpu_astaroth.cc:2283). */
+void testBCs(void);
+/* gpu_astaroth_ansi.c:44 -- split updates are not part of this path (no-op). */
+void splitUpdate(const REAL_PCGB eps, const int max_iter);
+/* gpu_astaroth_ansi.c:45 -- device pointers of the input and output f buffers. */
+void copyVBApointers(REAL_PCGB** in, REAL_PCGB** out);
+
+/* gpu_astaroth_ansi.c:48-56 -- TorchFort hooks: not part of this path (no-ops). */
+void tf_save_checkpoint_c_api(const char* a, const char* b);
+void tf_save_model_c_api(const char* a, const char* b);
+void tf_load_model_c_api(const char* a, const char* b);
+void tf_load_model_checkpoint_c_api(const char* a, const char* b);
+void tf_create_model_c_api(const char* a, const char* b, int comm, bool lmpicomm);
+void tf_train_c_api(const char* a, REAL_PCGB* loss, int itsub, double t);
+void tf_infer_c_api(const char* a, int itsub);
+void print_debug(void);
+
+/* Fortran-callable wrappers, gpu_astaroth_ansi.c:72-289 (gfortran: name_). */
+void initialize_gpu_c_(REAL_PCGB* f, int* comm, double* t, int* nt, int* read_all, int* cpu_dt, int* autotune);
+void register_gpu_c_(void);
+void finalize_gpu_c_(void);
+void get_farray_ptr_gpu_c_(REAL_PCGB** in, REAL_PCGB** out);
+void before_boundary_gpu_c_(int* lrmv, int* isubstep, double* t, int* lsubstepping);
+void update_after_substep_gpu_c_(void);
+void rhs_gpu_c_(int* isubstep, double* t);
+void copy_farray_c_(REAL_PCGB* f);
+void load_farray_c_(void);
+void reload_gpu_config_c_(void);
+void update_on_gpu_scal_by_ind_c_(int* index, REAL_PCGB* value);
+void update_on_gpu_vec_by_ind_c_(int* index, REAL_PCGB* value);
+void update_on_gpu_arr_by_ind_c_(int* index);
+int update_on_gpu_scal_by_name_c_(char* name, REAL_PCGB* value);
+int update_on_gpu_vec_by_name_c_(char* name, REAL_PCGB* value);
+int update_on_gpu_arr_by_name_c_(char* name);
+void gpu_prepare_for_first_substep_c_(double* t);
+void radtransfer_gpu_c_(void);
+void get_gpu_reduced_vars_c_(REAL_PCGB* dst);
+void test_bcs_c_(void);
+void split_update_gpu_c_(void);
+
+/* Timestep of the plug-in's box: the value Fortran's set_dt would receive
+   (gpu_astaroth.cc:1618-1634 calls set_dt from C++; a C caller reads it). */
+double pcgb_get_dt(void);
+double pcgb_get_time(void);
+/* Request device diagnostics (urms, brms, ...) on the next substep 1. */
+void pcgb_request_diagnostics(void);
+
+/* Timestep driver mirroring Timestep.time_step with lgpu=T
+   (src/timestep.f90:206 -> advance_substeps :77): nsteps full RK3 steps of
+   the plug-in box, substepGPU(1..3) each.  Returns 0 or an error code. */
+int pcgb_time_step(int nsteps);
+
+/* ---------------------------------------------------------------------------
+ * 2. Boxes, batches and serving (no reference counterpart: the reference
+ *    drives one domain per process).
+ * ------------------------------------------------------------------------- */
+typedef struct pcgb_box pcgb_box;
+typedef struct pcgb_batch pcgb_batch;
+
+pcgb_box* pcgb_box_create(const pcgb_params* p);
+void pcgb_box_destroy(pcgb_box* b);
+/* f(mx,my,mz,nf) double, Fortran order, ghosts included (ghosts are refreshed on device). */
+int pcgb_box_load(pcgb_box* b, const double* f_host, double t);
+int pcgb_box_store(pcgb_box* b, double* f_host);
+/* Seeded initial condition written on the device (for boxes too large to
+   stage through host memory): kind 0 sets field to zero, 1 adds ampl*N(0,1)
+   from a counter-based generator seeded by seed, 2 adds component `field`
+   (0..2) of the ABC flow (hydro.f90:2214-2220) ampl*(a,b,c) at wavenumber k.
+   Ghosts, df and the step bookkeeping are reset as after pcgb_box_load. */
+int pcgb_box_init_field(pcgb_box* b, int field, int kind, double ampl, double a, double bb, double c, double k,
+                        unsigned long long seed);
+/* Run nsteps RK3 steps (3 launches each, or 4 with dt_mode = 2). */
+int pcgb_box_steps(pcgb_box* b, int nsteps);
+int pcgb_box_sync(pcgb_box* b);
+/* out[0..PCGB_NSLOT-1] raw reduced slots, then t, dt, step of the diagnostics. */
+int pcgb_box_diag(pcgb_box* b, double* out, int nout);
+int pcgb_box_time(pcgb_box* b, double* t, double* dt, long long* nsub);
+int pcgb_box_set_dt(pcgb_box* b, double dt);
+/* Device bytes held by the box. */
+size_t pcgb_box_bytes(const pcgb_box* b);
+/* Cells, fields, precision and tile of the box. */
+int pcgb_box_info(const pcgb_box* b, int* info, int ninfo);
+
+/* A batch advances many boxes of one class (precision, field count, tile)
+   in one persistent launch per substep. */
+pcgb_batch* pcgb_batch_create(pcgb_box** boxes, int n, int persistent);
+void pcgb_batch_destroy(pcgb_batch* b);
+/* nsteps RK3 steps for every box; use_graph != 0 captures the substep loop
+   of graph_steps steps in a CUDA graph and replays it. */
+int pcgb_batch_steps(pcgb_batch* b, int nsteps, int use_graph, int graph_steps);
+
+/* Autotuner: times each tile variant and z-depth for a box of this shape and
+   returns the best (tile, zdepth); results are cached per (precision, nf, n). */
+int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, double* ms_per_substep);
+
+/* Number of kernel launches issued by this process (all entry points). */
+long long pcgb_launch_count(void);
+/* Name of the compiled device architecture and library version. */
+const char* pcgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

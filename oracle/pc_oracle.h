@@ -1,0 +1,80 @@
+/*
+ * pc_oracle.h -- CPU FP64 restatement of the Pencil Code compressible-MHD
+ * timestep (the pde() right-hand side + 2N-storage RK3 update).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity oracle: it is linked
+ * by tests/, by __graft_entry__.smoke() and by the CPU-baseline leg of
+ * bench.py, always as the checker and never as the thing measured or shipped.
+ * The product (libpcgb300.so) does not link it and has no CPU fallback.
+ *
+ * Layout: f(mx,my,mz,nf) Fortran column-major, x fastest, ghosts included
+ * (nghost = 3), exactly the reference f-array (src/cparam.f90:19-59).
+ * Variable order (src/register.f90:138-146): uu(1:3), lnrho, [ss], aa(1:3).
+ */
+#ifndef PC_ORACLE_H
+#define PC_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_NGHOST 3
+
+typedef struct {
+  int nx, ny, nz;           /* interior cells */
+  int lentropy;             /* 0: noentropy (7 fields), 1: entropy (8 fields) */
+  double x0, y0, z0;        /* xyz0 (cdata.f90:211 default -pi) */
+  double Lx, Ly, Lz;        /* Lxyz (default 2 pi) */
+  double gamma, cs0, rho0, cp;
+  double nu, eta, chi, mu0;
+  int lforcing_cont;        /* ABC continuous forcing into duu */
+  double ampl_ff, kf, relhel, abc_a, abc_b, abc_c, ampl_fcont_uu;
+  double b_ext[3];
+  int lohmic_heat, lviscosity_heat;
+  double cdt, cdtv;
+} orc_params;
+
+/* Diagnostic slots (FP64), evaluated on f at the start of a step. */
+enum {
+  ORC_D_U2SUM = 0, ORC_D_U2MAX, ORC_D_B2SUM, ORC_D_B2MAX, ORC_D_EKINSUM,
+  ORC_D_RHOSUM, ORC_D_DIVB2SUM, ORC_D_J2SUM, ORC_D_ABSUM, ORC_D_N
+};
+
+int  orc_nfields(const orc_params* p);
+void orc_grid(const orc_params* p, double* x, double* y, double* z);
+
+/* Periodic ghost filling, x then y then z (src/boundcond.f90:2387-2531). */
+void orc_ghosts_periodic(const orc_params* p, double* f, int nf);
+
+/* Stencils on a single interior point (0-based ghosted indices l,m,n),
+   field k, direction j (0,1,2).  deriv.f90:89 / :472 / :1367. */
+double orc_der(const orc_params* p, const double* f, int k, int j, int l, int m, int n);
+double orc_der2(const orc_params* p, const double* f, int k, int j, int l, int m, int n);
+double orc_derij(const orc_params* p, const double* f, int k, int i, int j, int l, int m, int n);
+
+/* Whole-interior stencil helpers used by the golden-vector tests:
+   out is (nx,ny,nz) x fastest.  kind: 0 der, 1 der2, 2 derij(i,j). */
+void orc_stencil_field(const orc_params* p, const double* f, int k, int kind, int i, int j,
+                       double* out);
+
+/* df(interior) = alpha*df + RHS(f).  f must have valid ghosts.
+   When want_dt: *dt1_max = max over cells of the CFL inverse timestep.
+   When diag != NULL: accumulates the ORC_D_* slots (sums and maxima). */
+void orc_pde(const orc_params* p, const double* f, double* df, double alpha,
+             int want_dt, double* dt1_max, double* diag, int nthreads);
+
+/* One full RK3 step (src/timestep.f90:77-202):  fills ghosts, runs the three
+   substeps, updates *t.  If ldt: dt is set from the CFL condition on substep
+   1 (src/sub.f90:4223) and returned through *dt.  diag may be NULL. */
+void orc_time_step(const orc_params* p, double* f, double* df, double* t, double* dt,
+                   int ldt, double* diag, int nthreads);
+
+/* The reference 'min_std' generator ran0 (src/general.f90:867-889) and
+   gaunoise_vect (src/initcond.f90:5005-5047). */
+double orc_ran0(int* state);
+void orc_gaunoise_vect(const orc_params* p, double ampl, double* f, int i1, int i2, int* state);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

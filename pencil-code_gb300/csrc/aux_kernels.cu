@@ -1,0 +1,186 @@
+// aux_kernels.cu -- layout conversion and ghost kernels used around the substep kernel.
+//
+// Host layout: the reference f-array f(mx,my,mz,nf), Fortran order, REAL=double,
+// mx = nx+6 (no padding).  Device layout: rows of px elements with interior
+// x = 0 at element xoff (ghosts at xoff-3 .. xoff-1 and xoff+nx .. xoff+nx+2),
+// so row r of the host array (r = m + my*(n + mz*k)) starts at element
+// px*r + xoff - 3 of the device array.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "aux_kernels.h"
+
+namespace pcgb {
+
+__device__ __forceinline__ int wrap(int i, int n) {  // ghosted index -> interior image, 0-based interior
+  int v = i - 3;
+  if (v < 0) v += n;
+  else if (v >= n) v -= n;
+  return v;
+}
+
+// Periodic ghost fill (boundcond.f90:2387-2531 bc_per_x/y/z): every ghost cell
+// takes the value of its interior image.  Reads interior cells only.
+template <typename T>
+__global__ void ghost_fill_kernel(T* __restrict__ f, int nx, int ny, int nz, int px, int my, int mz, int xoff,
+                                  int nf) {
+  const int mx = nx + 6;
+  const long long total = (long long)mx * my * mz * nf;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q % mx);
+    long long r = q / mx;
+    const int j = (int)(r % my);
+    r /= my;
+    const int k = (int)(r % mz);
+    const int fld = (int)(r / mz);
+    const bool ghost = (i < 3) | (i >= nx + 3) | (j < 3) | (j >= ny + 3) | (k < 3) | (k >= nz + 3);
+    if (!ghost) continue;
+    const long long fo = (long long)fld * px * my * mz;
+    const long long src = fo + (long long)(wrap(k, nz) + 3) * px * my + (long long)(wrap(j, ny) + 3) * px + xoff + wrap(i, nx);
+    const long long dst = fo + (long long)k * px * my + (long long)j * px + xoff - 3 + i;
+    f[dst] = f[src];
+  }
+}
+
+// Rows [r0, r0+nr) of the host layout (double) -> device layout (T).
+template <typename T>
+__global__ void load_rows_kernel(T* __restrict__ f, const double* __restrict__ stage, long long r0, long long nr, int mx,
+                                 int px, int xoff) {
+  const long long total = nr * mx;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long r = q / mx;
+    const int i = (int)(q - r * mx);
+    f[(r0 + r) * px + xoff - 3 + i] = (T)stage[q];
+  }
+}
+
+// Device layout (T) -> host-layout rows (double).  With a carry array (FP32
+// compensated mode), the value returned is f + carry of the interior image.
+template <typename T>
+__global__ void store_rows_kernel(double* __restrict__ stage, const T* __restrict__ f, const T* __restrict__ carry,
+                                  long long r0, long long nr, int nx, int ny, int nz, int px, int my, int mz,
+                                  int xoff) {
+  const int mx = nx + 6;
+  const long long total = nr * mx;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long r = q / mx;
+    const int i = (int)(q - r * mx);
+    const long long row = r0 + r;
+    double v = (double)f[row * px + xoff - 3 + i];
+    if (carry) {
+      const int j = (int)(row % my);
+      long long rr = row / my;
+      const int k = (int)(rr % mz);
+      const long long fld = rr / mz;
+      const long long ci = fld * px * my * mz + (long long)(wrap(k, nz) + 3) * px * my + (long long)(wrap(j, ny) + 3) * px +
+                           xoff + wrap(i, nx);
+      v += (double)carry[ci];
+    }
+    stage[q] = v;
+  }
+}
+
+static int grid_for(long long n, int threads) {
+  long long g = (n + threads - 1) / threads;
+  if (g > 65535LL * 16) g = 65535LL * 16;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+cudaError_t launch_ghost_fill(int tbytes, void* f, int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf,
+                              cudaStream_t s) {
+  const long long n = (long long)(nx + 6) * my * mz * nf;
+  const int th = 256, g = grid_for(n, th);
+  if (tbytes == 4)
+    ghost_fill_kernel<float><<<g, th, 0, s>>>((float*)f, nx, ny, nz, px, my, mz, xoff, nf);
+  else
+    ghost_fill_kernel<double><<<g, th, 0, s>>>((double*)f, nx, ny, nz, px, my, mz, xoff, nf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_load_rows(int tbytes, void* f, const double* stage, long long r0, long long nr, int mx, int px,
+                             int xoff, cudaStream_t s) {
+  const int th = 256, g = grid_for(nr * mx, th);
+  if (tbytes == 4)
+    load_rows_kernel<float><<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, px, xoff);
+  else
+    load_rows_kernel<double><<<g, th, 0, s>>>((double*)f, stage, r0, nr, mx, px, xoff);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_store_rows(int tbytes, double* stage, const void* f, const void* carry, long long r0, long long nr,
+                              int nx, int ny, int nz, int px, int my, int mz, int xoff, cudaStream_t s) {
+  const int th = 256, g = grid_for(nr * (nx + 6), th);
+  if (tbytes == 4)
+    store_rows_kernel<float><<<g, th, 0, s>>>(stage, (const float*)f, (const float*)carry, r0, nr, nx, ny, nz, px, my,
+                                              mz, xoff);
+  else
+    store_rows_kernel<double><<<g, th, 0, s>>>(stage, (const double*)f, (const double*)carry, r0, nr, nx, ny, nz, px,
+                                               my, mz, xoff);
+  return cudaGetLastError();
+}
+
+}  // namespace pcgb
+
+namespace pcgb {
+
+// splitmix64 (Steele, Lea & Flood 2014), used as a counter-based generator.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// Seeded initial conditions written on the device into one field's interior:
+// kind 0: set to zero; 1: add ampl * N(0,1) (Box-Muller on two counter-based
+// uniforms); 2: add the ABC flow component fld (hydro.f90:2214-2220) with
+// amplitudes a,b,c and wavenumber k on the cell-centred grid.
+template <typename T>
+__global__ void init_field_kernel(T* __restrict__ f, int kind, int comp, double ampl, double a, double b, double c,
+                                  double k, unsigned long long seed, int nx, int ny, int nz, int px, int my, int xoff,
+                                  double x0, double y0, double z0, double dx, double dy, double dz) {
+  const long long total = (long long)nx * ny * nz;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q % nx);
+    const long long r = q / nx;
+    const int j = (int)(r % ny);
+    const int kk = (int)(r / ny);
+    const long long idx = (long long)(kk + 3) * px * my + (long long)(j + 3) * px + xoff + i;
+    if (kind == 0) {
+      f[idx] = T(0);
+    } else if (kind == 1) {
+      const unsigned long long h1 = splitmix64(seed * 0x100000001B3ull + 2ull * (unsigned long long)q);
+      const unsigned long long h2 = splitmix64(h1 ^ 0xD1B54A32D192ED03ull);
+      const double u1 = ((double)(h1 >> 11) + 1.0) * (1.0 / 9007199254740993.0);   // (0,1]
+      const double u2 = (double)(h2 >> 11) * (1.0 / 9007199254740992.0);            // [0,1)
+      const double g = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+      f[idx] = (T)((double)f[idx] + ampl * g);
+    } else {
+      const double x = x0 + ((double)i + 0.5) * dx, y = y0 + ((double)j + 0.5) * dy, z = z0 + ((double)kk + 0.5) * dz;
+      double v;
+      if (comp == 0) v = a * sin(k * z) + c * cos(k * y);
+      else if (comp == 1) v = b * sin(k * x) + a * cos(k * z);
+      else v = c * sin(k * y) + b * cos(k * x);
+      f[idx] = (T)((double)f[idx] + ampl * v);
+    }
+  }
+}
+
+cudaError_t launch_init_field(int tbytes, void* f, int kind, int comp, double ampl, double a, double b, double c,
+                              double k, unsigned long long seed, int nx, int ny, int nz, int px, int my, int xoff,
+                              double x0, double y0, double z0, double dx, double dy, double dz, cudaStream_t s) {
+  const int th = 256, g = grid_for((long long)nx * ny * nz, th);
+  if (tbytes == 4)
+    init_field_kernel<float><<<g, th, 0, s>>>((float*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my, xoff,
+                                              x0, y0, z0, dx, dy, dz);
+  else
+    init_field_kernel<double><<<g, th, 0, s>>>((double*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my,
+                                               xoff, x0, y0, z0, dx, dy, dz);
+  return cudaGetLastError();
+}
+
+}  // namespace pcgb

@@ -1,0 +1,56 @@
+"""Shared test setup: the `gpu` marker, import paths, and helpers that build
+matching parameter blocks for the CUDA library and the FP64 oracle."""
+import importlib
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a GB300 (sm_103a) GPU and the CUDA library")
+
+
+@pytest.fixture(scope="session")
+def pc():
+    return importlib.import_module("pencil-code_gb300")
+
+
+@pytest.fixture(scope="session")
+def ic():
+    return importlib.import_module("pencil-code_gb300.initcond")
+
+
+@pytest.fixture(scope="session")
+def orc():
+    import oracle
+    oracle.build()
+    return oracle
+
+
+def oracle_params(orc, p):
+    """Oracle parameter block equal to a library Params block."""
+    return orc.make_params(
+        nx=p.nx, ny=p.ny, nz=p.nz, lentropy=p.lentropy,
+        x0=p.xyz0[0], y0=p.xyz0[1], z0=p.xyz0[2], Lx=p.Lxyz[0], Ly=p.Lxyz[1], Lz=p.Lxyz[2],
+        gamma=p.gamma, cs0=p.cs0, rho0=p.rho0, cp=p.cp, nu=p.nu, eta=p.eta, chi=p.chi, mu0=p.mu0,
+        lforcing_cont=p.lforcing_cont, ampl_ff=p.ampl_ff, kf=p.kf, relhel=p.relhel,
+        abc_a=p.abc_a, abc_b=p.abc_b, abc_c=p.abc_c, ampl_fcont_uu=p.ampl_fcont_uu,
+        b_ext=tuple(p.b_ext), lohmic_heat=p.lohmic_heat, lviscosity_heat=p.lviscosity_heat,
+        cdt=p.cdt, cdtv=p.cdtv)
+
+
+def rel_err(a, b):
+    """Per-field max |a-b| / max |b| (interior only)."""
+    out = []
+    for k in range(a.shape[3]):
+        A = a[3:-3, 3:-3, 3:-3, k]
+        B = b[3:-3, 3:-3, 3:-3, k]
+        scale = np.max(np.abs(B))
+        out.append(np.max(np.abs(A - B)) / scale if scale > 0 else np.max(np.abs(A - B)))
+    return np.array(out)

@@ -1,0 +1,189 @@
+"""Parity of the CUDA substep kernel (through the C ABI) with the FP64 oracle.
+
+Tolerances (max |gpu - oracle| / max |oracle| per field):
+  FP64 state: 1e-11 on fields after the run, 1e-12 on diagnostics;
+  FP32 compensated state: 1e-5 on fields.
+"""
+import numpy as np
+import pytest
+
+from conftest import oracle_params, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-11
+TOLDIAG = 1e-12
+TOL32 = 1e-5
+
+
+def iso_params(pc, n=32, **kw):
+    p = pc.default_params(nx=n, ny=n, nz=n, gamma=1.0, nu=5e-3, eta=5e-3, dt=5e-3, precision=8)
+    return p.update(**kw)
+
+
+def iso_state(pc, ic, p, ampl=1e-3, seed=1):
+    f = ic.zeros(p)
+    ic.gaussian_noise(f, p, ["ux", "uy", "uz", "ax", "ay", "az"], ampl, seed)
+    return f
+
+
+def run_oracle(orc, p, f0, nsteps, ldt=False, dt=None):
+    op = oracle_params(orc, p)
+    f = np.array(f0, order="F", copy=True)
+    df = np.zeros_like(f)
+    t, d = 0.0, (p.dt if dt is None else dt)
+    for _ in range(nsteps):
+        t, d, _ = orc.time_step(op, f, df, t, d, ldt, nthreads=8)
+    orc.ghosts(op, f)
+    return f, t, d
+
+
+def test_isothermal_fp64_100_steps(pc, ic, orc):
+    """32^3 isothermal MHD, FP64, fixed dt=5e-3, 100 steps (the 32^3 FP64 parity case)."""
+    p = iso_params(pc)
+    f0 = iso_state(pc, ic, p)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(100)
+    g = box.store()
+    ref, t_ref, _ = run_oracle(orc, p, f0, 100)
+    err = rel_err(g, ref)
+    assert np.all(err <= TOL64), err
+    t, dt, nsub = box.time()
+    assert nsub % 3 == 0 and abs(t - t_ref) <= 1e-12 * t_ref
+    # ghosts of the stored f are the exact periodic images
+    gg = ic.fill_ghosts(g.copy())
+    assert np.array_equal(gg, g)
+
+
+def test_entropy_fp64_abc(pc, ic, orc):
+    """8 fields with entropy, ABC initial flow, Ohmic/viscous heating, chi-const conduction."""
+    p = pc.default_params(nx=32, ny=32, nz=32, lentropy=1, gamma=5.0 / 3.0, nu=2e-3, eta=2e-3, chi=2e-3,
+                          dt=1e-3, precision=8)
+    f0 = ic.zeros(p)
+    ic.abc_flow(f0, p, ampl=1.0, A=0.1, B=0.1, C=0.1, k=1.0)
+    ic.gaussian_noise(f0, p, ["ax", "ay", "az"], 1e-4, 7)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(20)
+    g = box.store()
+    ref, _, _ = run_oracle(orc, p, f0, 20)
+    err = rel_err(g, ref)
+    assert np.all(err <= TOL64), err
+
+
+def test_forcing_bext_polytropic(pc, ic, orc):
+    """ABC continuous forcing, imposed B_ext, polytropic (gamma != 1 without entropy), non-cubic grid."""
+    p = pc.default_params(nx=48, ny=32, nz=40, gamma=1.4, nu=1e-2, eta=2e-2, dt=2e-3, precision=8,
+                          lforcing_cont=1, ampl_ff=0.05, kf=2.0, relhel=0.5, abc_a=1.0, abc_b=0.7, abc_c=0.3,
+                          b_ext=(0.0, 0.1, 0.05))
+    p.update(Lxyz=(2 * np.pi, 1.5 * np.pi, 2.5 * np.pi))
+    f0 = iso_state(pc, ic, p, ampl=1e-2, seed=3)
+    ic.gaussian_noise(f0, p, ["lnrho"], 1e-3, 4)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(10)
+    g = box.store()
+    ref, _, _ = run_oracle(orc, p, f0, 10)
+    assert np.all(rel_err(g, ref) <= TOL64)
+
+
+def test_cfl_current_semantics(pc, ic, orc):
+    """dt from the CFL condition of the current f (CPU semantics, lcpu_timestep_on_gpu)."""
+    p = iso_params(pc, dt=0.0, dt_mode=2, cdt=0.4, b_ext=(0.0, 0.1, 0.0), nu=0.05, eta=0.05)
+    f0 = iso_state(pc, ic, p, ampl=1e-2, seed=5)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(10)
+    g = box.store()
+    t, dt, _ = box.time()
+    ref, t_ref, dt_ref = run_oracle(orc, p, f0, 10, ldt=True, dt=0.0)
+    assert np.all(rel_err(g, ref) <= TOL64)
+    assert abs(dt - dt_ref) <= 1e-13 * dt_ref and abs(t - t_ref) <= 1e-13 * t_ref
+
+
+def test_cfl_lagged_semantics(pc, ic, orc):
+    """Reference GPU default: dt of step n is the CFL of f at the start of step n-1
+    (the first step uses the CFL of the initial f)."""
+    p = iso_params(pc, dt=0.0, dt_mode=1, cdt=0.4, nu=0.05, eta=0.05)
+    f0 = iso_state(pc, ic, p, ampl=1e-2, seed=6)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(6)
+    g = box.store()
+    op = oracle_params(orc, p)
+    f = np.array(f0, order="F", copy=True)
+    df = np.zeros_like(f)
+    orc.ghosts(op, f)
+    dt1, _ = orc.pde(op, f, np.zeros_like(f), 0.0, want_dt=True)
+    dt_use = 1.0 / dt1
+    t = 0.0
+    for _ in range(6):
+        orc.ghosts(op, f)
+        d1, _ = orc.pde(op, f, np.zeros_like(f), 0.0, want_dt=True)
+        t, _, _ = orc.time_step(op, f, df, t, dt_use, False, nthreads=8)
+        dt_use = 1.0 / d1
+    orc.ghosts(op, f)
+    assert np.all(rel_err(g, f) <= TOL64)
+
+
+def test_diagnostics_fp64(pc, ic, orc):
+    p = iso_params(pc, diag_every=1, b_ext=(0.0, 0.1, 0.0))
+    f0 = iso_state(pc, ic, p, ampl=1e-2, seed=8)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(1)
+    raw = box.diag_raw()
+    op = oracle_params(orc, p)
+    f = np.array(f0, order="F", copy=True)
+    orc.ghosts(op, f)
+    _, dg = orc.pde(op, f, np.zeros_like(f), 0.0, diag=True)
+    for k in range(9):
+        ref = dg[k]
+        got = raw[k + 1]
+        assert abs(got - ref) <= TOLDIAG * max(abs(ref), 1e-300), (k, got, ref)
+
+
+def test_isothermal_fp32_compensated(pc, ic, orc):
+    """FP32 state with the compensated 2N accumulation, within 1e-5 of the FP64 oracle."""
+    p = iso_params(pc, precision=4, comp=1)
+    p.update(nu=5e-3, eta=5e-3)
+    f0 = iso_state(pc, ic, p)
+    ic.abc_flow(f0, p, ampl=0.1)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(100)
+    g = box.store()
+    ref, _, _ = run_oracle(orc, p, f0, 100)
+    err = rel_err(g, ref)
+    assert np.all(err <= TOL32), err
+
+
+def test_entropy_fp32(pc, ic, orc):
+    p = pc.default_params(nx=32, ny=32, nz=32, lentropy=1, gamma=5.0 / 3.0, nu=2e-3, eta=2e-3, chi=2e-3,
+                          dt=1e-3, precision=4, comp=1)
+    f0 = ic.zeros(p)
+    ic.abc_flow(f0, p, ampl=1.0, A=0.1, B=0.1, C=0.1, k=1.0)
+    ic.gaussian_noise(f0, p, ["ax", "ay", "az"], 1e-4, 7)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(20)
+    g = box.store()
+    ref, _, _ = run_oracle(orc, p, f0, 20)
+    assert np.all(rel_err(g, ref) <= TOL32)
+
+
+@pytest.mark.parametrize("tile", [0, 1, 2, 3])
+def test_tile_variants_agree(pc, ic, tile):
+    """Every tile variant and z-depth gives bitwise the same FP64 result."""
+    base = None
+    for zd in (0, 8):
+        p = iso_params(pc, n=32, tile=tile, zdepth=zd)
+        f0 = iso_state(pc, ic, p, seed=11)
+        box = pc.Box(p)
+        box.load(f0)
+        box.steps(3)
+        g = box.store()
+        if base is None:
+            base = g
+        assert np.array_equal(g, base)
