@@ -110,6 +110,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "pcgb_get_stream": (vp, []),
         "initializeGPU": (None, [dptr, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int]),
         "substepGPU": (None, [C.c_int, C.c_double]),
+        "beforeBoundaryGPU": (None, [C.c_bool, C.c_int, C.c_double, C.c_bool]),
+        "afterSubStepGPU": (None, []),
+        "registerGPU": (None, []),
         "copyFarray": (None, [dptr]),
         "loadFarray": (None, []),
         "finalizeGPU": (None, []),

@@ -45,12 +45,22 @@ def oracle_params(orc, p):
         cdt=p.cdt, cdtv=p.cdtv)
 
 
-def rel_err(a, b):
-    """Per-field max |a-b| / max |b| (interior only)."""
+def rel_err(a, b, log_fields=()):
+    """Per-field max |a-b| / scale over the interior, scale = max |b|.
+
+    For the logarithmic variables (lnrho, ss; indices in log_fields) the scale
+    is max(max |b|, 1): an absolute error in ln(rho) is the relative error of
+    rho, and ss is in units of cp = 1."""
     out = []
     for k in range(a.shape[3]):
         A = a[3:-3, 3:-3, 3:-3, k]
         B = b[3:-3, 3:-3, 3:-3, k]
         scale = np.max(np.abs(B))
+        if k in log_fields:
+            scale = max(scale, 1.0)
         out.append(np.max(np.abs(A - B)) / scale if scale > 0 else np.max(np.abs(A - B)))
     return np.array(out)
+
+
+LOG7 = (3,)       # lnrho in the 7-field (isothermal) f-array
+LOG8 = (3, 4)     # lnrho, ss in the 8-field (entropy) f-array

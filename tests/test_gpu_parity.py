@@ -2,12 +2,16 @@
 
 Tolerances (max |gpu - oracle| / max |oracle| per field):
   FP64 state: 1e-11 on fields after the run, 1e-12 on diagnostics;
-  FP32 compensated state: 1e-5 on fields.
+  FP32 compensated state: 1e-5 on fields, where lnrho and ss are measured
+  against max(max|field|, 1) (an absolute error in ln rho is the relative
+  error of rho).
+div B is zero up to round-off in both codes; it is checked against the
+current density scale instead of relatively.
 """
 import numpy as np
 import pytest
 
-from conftest import oracle_params, rel_err
+from conftest import LOG7, LOG8, oracle_params, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -141,6 +145,10 @@ def test_diagnostics_fp64(pc, ic, orc):
     for k in range(9):
         ref = dg[k]
         got = raw[k + 1]
+        if k == orc.D_DIVB2SUM:
+            # round-off only: |div B| <= 1e-12 |J| in both codes
+            assert got <= 1e-24 * dg[orc.D_J2SUM] and ref <= 1e-24 * dg[orc.D_J2SUM]
+            continue
         assert abs(got - ref) <= TOLDIAG * max(abs(ref), 1e-300), (k, got, ref)
 
 
@@ -155,7 +163,7 @@ def test_isothermal_fp32_compensated(pc, ic, orc):
     box.steps(100)
     g = box.store()
     ref, _, _ = run_oracle(orc, p, f0, 100)
-    err = rel_err(g, ref)
+    err = rel_err(g, ref, LOG7)
     assert np.all(err <= TOL32), err
 
 
@@ -170,7 +178,8 @@ def test_entropy_fp32(pc, ic, orc):
     box.steps(20)
     g = box.store()
     ref, _, _ = run_oracle(orc, p, f0, 20)
-    assert np.all(rel_err(g, ref) <= TOL32)
+    err = rel_err(g, ref, LOG8)
+    assert np.all(err <= TOL32), err
 
 
 @pytest.mark.parametrize("tile", [0, 1, 2, 3])
@@ -186,4 +195,18 @@ def test_tile_variants_agree(pc, ic, tile):
         g = box.store()
         if base is None:
             base = g
-        assert np.array_equal(g, base)
+        assert np.array_equal(g, base)   # z-depth never changes the arithmetic
+
+
+def test_tiles_cross_agree(pc, ic):
+    """Different tile shapes agree to round-off (FMA contraction may differ per variant)."""
+    outs = []
+    for tile in range(4):
+        p = iso_params(pc, n=32, tile=tile)
+        f0 = iso_state(pc, ic, p, seed=12)
+        box = pc.Box(p)
+        box.load(f0)
+        box.steps(3)
+        outs.append(box.store())
+    for g in outs[1:]:
+        assert np.all(rel_err(g, outs[0]) <= 1e-14)
