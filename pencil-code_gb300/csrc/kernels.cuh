@@ -8,7 +8,8 @@ namespace pcgb {
 // Tile variants (TX, TY).  The ring depth is fixed per precision.
 struct TileShape { int tx, ty; };
 constexpr int kNumTiles = 4;
-// FP32 variants: (32,4) (32,8) (16,8) (64,4); FP64 variants: (32,4) (16,8) (16,4) (32,2)
+// FP32 variants: (32,4) (32,8) (16,8) (64,4); FP64 variants: (32,4) (16,8) (16,4) (32,2).
+// FP32 (32,4) and (16,8) ask for two resident CTAs per SM.
 inline TileShape tile_shape(int dtype_bytes, int tile) {
   static const TileShape f32[kNumTiles] = {{32, 4}, {32, 8}, {16, 8}, {64, 4}};
   static const TileShape f64[kNumTiles] = {{32, 4}, {16, 8}, {16, 4}, {32, 2}};
@@ -38,14 +39,14 @@ inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile) {
 // Instantiation helper used by the kernels_*.cu translation units.
 #define PCGB_DEFINE_KERNELS(NAME, T, NF)                                                   \
   namespace pcgb {                                                                         \
-  template <int TX, int TY>                                                                \
+  template <int TX, int TY, int MB>                                                        \
   static KernelHandle make_##NAME() {                                                      \
     constexpr int R = ring_depth(sizeof(T));                                               \
     KernelHandle h;                                                                        \
-    h.fn = reinterpret_cast<const void*>(&mhd_substep_kernel<T, NF, TX, TY, R>);           \
+    h.fn = reinterpret_cast<const void*>(&mhd_substep_kernel<T, NF, TX, TY, R, MB>);       \
     h.smem = TileCfg<T, NF, TX, TY, R>::SMEM_BYTES;                                        \
     h.threads = TX * TY;                                                                   \
-    cudaFuncSetAttribute(&mhd_substep_kernel<T, NF, TX, TY, R>,                            \
+    cudaFuncSetAttribute(&mhd_substep_kernel<T, NF, TX, TY, R, MB>,                        \
                          cudaFuncAttributeMaxDynamicSharedMemorySize, h.smem);             \
     return h;                                                                              \
   }                                                                                        \
@@ -56,17 +57,17 @@ inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile) {
     if (!init[tile]) {                                                                     \
       if constexpr (sizeof(T) == 4) {                                                      \
         switch (tile) {                                                                    \
-          case 0: cache[0] = make_##NAME<32, 4>(); break;                                  \
-          case 1: cache[1] = make_##NAME<32, 8>(); break;                                  \
-          case 2: cache[2] = make_##NAME<16, 8>(); break;                                  \
-          default: cache[3] = make_##NAME<64, 4>(); break;                                 \
+          case 0: cache[0] = make_##NAME<32, 4, 2>(); break;                               \
+          case 1: cache[1] = make_##NAME<32, 8, 1>(); break;                               \
+          case 2: cache[2] = make_##NAME<16, 8, 2>(); break;                               \
+          default: cache[3] = make_##NAME<64, 4, 1>(); break;                              \
         }                                                                                  \
       } else {                                                                             \
         switch (tile) {                                                                    \
-          case 0: cache[0] = make_##NAME<32, 4>(); break;                                  \
-          case 1: cache[1] = make_##NAME<16, 8>(); break;                                  \
-          case 2: cache[2] = make_##NAME<16, 4>(); break;                                  \
-          default: cache[3] = make_##NAME<32, 2>(); break;                                 \
+          case 0: cache[0] = make_##NAME<32, 4, 1>(); break;                               \
+          case 1: cache[1] = make_##NAME<16, 8, 1>(); break;                               \
+          case 2: cache[2] = make_##NAME<16, 4, 1>(); break;                               \
+          default: cache[3] = make_##NAME<32, 2, 1>(); break;                              \
         }                                                                                  \
       }                                                                                    \
       init[tile] = true;                                                                   \

@@ -157,8 +157,8 @@ __device__ __forceinline__ T cfl_dt1(const Phys<T>& P, const Fac<T>& F, const T 
   return tsqrt(a * a + d * d);
 }
 
-template <typename T, int NF, int TX, int TY, int RING>
-__global__ void __launch_bounds__(TX* TY, 1) mhd_substep_kernel(LaunchArgs args) {
+template <typename T, int NF, int TX, int TY, int RING, int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs args) {
   using C = TileCfg<T, NF, TX, TY, RING>;
   constexpr int IUX = 0, ILNRHO = 3, ISS = 4, IAX = NF - 3;
   constexpr bool ENTROPY = (NF == 8);
@@ -277,6 +277,21 @@ __global__ void __launch_bounds__(TX* TY, 1) mhd_substep_kernel(LaunchArgs args)
     const T* sinz = cosy + bmy;
     const T* cosz = sinz + bmz;
 
+    // forcing factors that depend on x or y only, read once per tile
+    T fsx = T(0), fcx = T(0), fsy = T(0), fcy = T(0);
+    if (blforcing && active) {
+      fsx = sinx[x + 3]; fcx = cosx[x + 3]; fsy = siny[y + 3]; fcy = cosy[y + 3];
+    }
+    // df of the first plane, prefetched; later planes are prefetched one plane ahead
+    T dfnext[NF];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) dfnext[k] = T(0);
+    if (read_df && active && !mode_cfl) {
+      const long long c0 = (long long)(z0 + 3) * bps + (long long)(y + 3) * bpx + bxoff + x;
+#pragma unroll
+      for (int k = 0; k < NF; ++k) dfnext[k] = dfp[k * bfs + c0];
+    }
+
     Acc acc;
     acc.reset();
     T dt1max = T(0);
@@ -313,12 +328,11 @@ __global__ void __launch_bounds__(TX* TY, 1) mhd_substep_kernel(LaunchArgs args)
         }
         const long long cidx = (long long)(z + 3) * bps + (long long)(y + 3) * bpx + bxoff + x;
         T dfo[NF];
-        if (read_df) {
 #pragma unroll
-          for (int k = 0; k < NF; ++k) dfo[k] = dfp[k * bfs + cidx];
-        } else {
+        for (int k = 0; k < NF; ++k) dfo[k] = dfnext[k];
+        if (read_df && z + 1 < z1) {
 #pragma unroll
-          for (int k = 0; k < NF; ++k) dfo[k] = T(0);
+          for (int k = 0; k < NF; ++k) dfnext[k] = dfp[k * bfs + cidx + bps];
         }
 
         // ---- hydro pencils (hydro.f90:3564-3990, sub.f90) ----
@@ -394,22 +408,35 @@ __global__ void __launch_bounds__(TX* TY, 1) mhd_substep_kernel(LaunchArgs args)
         bb[0] = aij[2][1] - aij[1][2];
         bb[1] = aij[0][2] - aij[2][0];
         bb[2] = aij[1][0] - aij[0][1];
-        // d2A[j][k][i] = A_i,jk
+        // d2A[j][k][i] = A_i,jk.  J = curl(b_ij) uses the six off-diagonal b_ij,
+        // which need the mixed derivatives A_1,xy A_2,xy A_1,xz A_3,xz A_2,yz A_3,yz;
+        // the other three (A_3,xy A_2,xz A_1,yz) enter only the diagonal b_ii,
+        // i.e. div B, and are evaluated on diagnostic substeps only.
         T d2A[3][3][3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
+        for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int jj = 0; jj < 3; ++jj) d2A[jj][jj][i] = st.der2(IAX + i, jj);
-          d2A[1][2][i] = st.derij(IAX + i, 1, 2); d2A[2][1][i] = d2A[1][2][i];
-          d2A[2][0][i] = st.derij(IAX + i, 0, 2); d2A[0][2][i] = d2A[2][0][i];
-          d2A[0][1][i] = st.derij(IAX + i, 0, 1); d2A[1][0][i] = d2A[0][1][i];
-        }
+        d2A[0][1][0] = st.derij(IAX + 0, 0, 1); d2A[1][0][0] = d2A[0][1][0];
+        d2A[0][1][1] = st.derij(IAX + 1, 0, 1); d2A[1][0][1] = d2A[0][1][1];
+        d2A[0][2][0] = st.derij(IAX + 0, 0, 2); d2A[2][0][0] = d2A[0][2][0];
+        d2A[0][2][2] = st.derij(IAX + 2, 0, 2); d2A[2][0][2] = d2A[0][2][2];
+        d2A[1][2][1] = st.derij(IAX + 1, 1, 2); d2A[2][1][1] = d2A[1][2][1];
+        d2A[1][2][2] = st.derij(IAX + 2, 1, 2); d2A[2][1][2] = d2A[1][2][2];
+        // off-diagonal b_ij = eps_ikl A_l,kj (sub.f90:3017-3019)
         T bij[3][3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          bij[0][k] = d2A[1][k][2] - d2A[2][k][1];
-          bij[1][k] = d2A[2][k][0] - d2A[0][k][2];
-          bij[2][k] = d2A[0][k][1] - d2A[1][k][0];
+        bij[0][1] = d2A[1][1][2] - d2A[2][1][1];
+        bij[0][2] = d2A[1][2][2] - d2A[2][2][1];
+        bij[1][0] = d2A[2][0][0] - d2A[0][0][2];
+        bij[1][2] = d2A[2][2][0] - d2A[0][2][2];
+        bij[2][0] = d2A[0][0][1] - d2A[1][0][0];
+        bij[2][1] = d2A[0][1][1] - d2A[1][1][0];
+        bij[0][0] = bij[1][1] = bij[2][2] = T(0);
+        if (want_diag) {
+          const T a3xy = st.derij(IAX + 2, 0, 1), a2xz = st.derij(IAX + 1, 0, 2), a1yz = st.derij(IAX + 0, 1, 2);
+          bij[0][0] = a3xy - a2xz;
+          bij[1][1] = a1yz - a3xy;
+          bij[2][2] = a2xz - a1yz;
         }
         T del2a[3];
 #pragma unroll
@@ -439,9 +466,9 @@ __global__ void __launch_bounds__(TX* TY, 1) mhd_substep_kernel(LaunchArgs args)
         for (int jj = 0; jj < 3; ++jj)
           dfu[jj] = dfu[jj] + P.nu * ((del2u[jj] + T(2) * sglnrho[jj]) + T(1.0 / 3.0) * graddivu[jj]);
         if (blforcing) {
-          const T fc0 = P.fact * (P.abc_c * sinz[z + 3] + (P.fact2 * P.abc_b) * cosy[y + 3]);
-          const T fc1 = P.fact * (P.abc_a * sinx[x + 3] + (P.fact2 * P.abc_c) * cosz[z + 3]);
-          const T fc2 = P.fact * (P.abc_b * siny[y + 3] + (P.fact2 * P.abc_a) * cosx[x + 3]);
+          const T fc0 = P.fact * (P.abc_c * sinz[z + 3] + (P.fact2 * P.abc_b) * fcy);
+          const T fc1 = P.fact * (P.abc_a * fsx + (P.fact2 * P.abc_c) * cosz[z + 3]);
+          const T fc2 = P.fact * (P.abc_b * fsy + (P.fact2 * P.abc_a) * fcx);
           dfu[0] = dfu[0] + P.ampl_fc * fc0;
           dfu[1] = dfu[1] + P.ampl_fc * fc1;
           dfu[2] = dfu[2] + P.ampl_fc * fc2;
