@@ -231,6 +231,43 @@ int pcgb_batch_steps(pcgb_batch* b, int nsteps, int use_graph, int graph_steps);
    returns the best (tile, zdepth); results are cached per (precision, nf, n). */
 int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, double* ms_per_substep);
 
+/* ---------------------------------------------------------------------------
+ * 3. Allocation-free substep (no counterpart in the reference).
+ *
+ * For callers that cannot allocate device memory at this point: a host code
+ * whose device memory belongs to another allocator (a caching pool holding the
+ * free memory, an application that reserves every buffer at start-up), or a
+ * time loop that must not incur the device-wide synchronisation that
+ * cudaMalloc/cudaFree can imply.  The caller owns f_in, f_out and df; the call
+ * allocates nothing (no cudaMalloc/cudaFree, no library allocator).
+ *
+ * Buffers use the library's device layout for the parameter block p:
+ * element (i, j, k, field), interior i in [0,nx), at
+ *   field*fs + (k+3)*ps + (j+3)*px + xoff + i,
+ *   xoff = 128/precision, px = xoff + roundup(nx+8, xoff), ps = px*(ny+6),
+ *   fs = ps*(nz+6)   (the same layout pcgb_box_info reports),
+ * each buffer fs*nf*precision bytes, 16-byte aligned.  f_in must hold valid
+ * periodic ghosts (every f_out written by this call does).  One call performs
+ * substep isubstep (1..3) of the 2N-RK3 scheme with timestep dt (FP64 or FP32
+ * state, without the FP32 carry): df is written on substeps 1-2 and read on
+ * 2-3.  If reductions != NULL (host array of PCGB_NSLOT doubles) the call waits
+ * for the kernel and returns, on substep 1, the CFL inverse timestep in [0]
+ * and the diagnostic slots (sums/maxima of u^2, B^2, ...) in [1..9].
+ * stream is a cudaStream_t (NULL: the default stream).
+ *
+ * Its scratch (descriptor, step state, forcing tables, per-tile partials) is
+ * a fixed file-scope device array of about 1.5 MB that every GPU using the
+ * library keeps until exit; limits: nx, ny, nz <= PCGB_NOALLOC_MAX_EXTENT and
+ * at most PCGB_NOALLOC_MAX_TILES tiles (larger requests return 7).  The first
+ * call on each device looks up the scratch address; make it before any stream
+ * capture.  All calls share the scratch: calls that overlap on the GPU race.
+ * Returns 0, or 2 (bad argument), 7 (size limit), 1 (CUDA error), 5 (device
+ * error flag). */
+#define PCGB_NOALLOC_MAX_EXTENT 4096
+#define PCGB_NOALLOC_MAX_TILES 16384
+int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double dt, const void* f_in, void* f_out, void* df,
+                         double* reductions, void* stream);
+
 /* Number of kernel launches issued by this process (all entry points). */
 long long pcgb_launch_count(void);
 /* Name of the compiled device architecture and library version. */

@@ -78,7 +78,7 @@ EXPORTS = [
     "pcgb_box_create", "pcgb_box_destroy", "pcgb_box_load", "pcgb_box_store", "pcgb_box_init_field", "pcgb_box_steps",
     "pcgb_box_sync", "pcgb_box_diag", "pcgb_box_time", "pcgb_box_set_dt", "pcgb_box_bytes",
     "pcgb_box_info", "pcgb_batch_create", "pcgb_batch_destroy", "pcgb_batch_steps", "pcgb_autotune",
-    "pcgb_launch_count", "pcgb_version",
+    "pcgb_launch_count", "pcgb_version", "pcgb_substep_noalloc",
 ]
 
 
@@ -144,6 +144,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "pcgb_batch_destroy": (None, [vp]),
         "pcgb_batch_steps": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
         "pcgb_autotune": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), dptr]),
+        "pcgb_substep_noalloc": (C.c_int, [P, C.c_int, C.c_double, vp, vp, vp, dptr, vp]),
         "pcgb_launch_count": (C.c_longlong, []),
         "pcgb_version": (C.c_char_p, []),
     }
