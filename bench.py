@@ -165,6 +165,22 @@ def cpu_oracle_rate(n: int, steps: int, threads: int, lentropy: int = 0) -> tupl
     return n ** 3 * 3 * steps / el / 1e9, el, {"n": n, "steps": steps}
 
 
+def max_over_ranks(ms: float, device=None) -> float:
+    """Slowest rank's time (the timed region ends when every replica is done)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(cells_per_rank: float, steps: int, world: int, ms: float) -> float:
+    """Gcell-updates/s per substep summed over all ranks (weak scaling: every rank owns a replica)."""
+    return world * cells_per_rank * 3 * steps / (ms / 1e3) / 1e9
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -234,12 +250,9 @@ def run_ours(args):
     ms, launches = time_box_steps(pc, torch, box, stream, args.steps)
     clocks = sampler.stop()
     box.sync()
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, device="cuda")
     cells = float(n) ** 3
-    value = ws * cells * 3 * args.steps / (ms / 1e3) / 1e9
+    value = whole_job_value(cells, args.steps, ws, ms)
     per_launch_ms = ms / launches if launches else float("nan")
     bpc = bytes_per_cell_substep(nf, prec, True)
     achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
