@@ -42,16 +42,32 @@ __global__ void ghost_fill_kernel(T* __restrict__ f, int nx, int ny, int nz, int
   }
 }
 
+// Device element of host-layout row `row` (r = m + my*(n + mz*field)), x index i
+// (0..mx-1): field-major layout (pairs == 0) or packed pairs (pairs == 1, see
+// cell_pair.cuh: P0=(ux,ax) P1=(uy,ay) P2=(uz,az) P3=(lnrho,ss)), in units of T.
+__device__ __forceinline__ long long dev_index(long long row, int i, int my, int mz, int px, int xoff, int nf,
+                                               int pairs) {
+  if (!pairs) return row * px + xoff - 3 + i;
+  const long long jk = row % ((long long)my * mz);
+  const int fld = (int)(row / ((long long)my * mz));
+  int pair, lane;
+  if (fld < 3) { pair = fld; lane = 0; }
+  else if (fld == 3) { pair = 3; lane = 0; }
+  else if (nf == 8 && fld == 4) { pair = 3; lane = 1; }
+  else { pair = fld - (nf - 3); lane = 1; }
+  return 2 * (((long long)pair * my * mz + jk) * px + xoff - 3 + i) + lane;
+}
+
 // Rows [r0, r0+nr) of the host layout (double) -> device layout (T).
 template <typename T>
 __global__ void load_rows_kernel(T* __restrict__ f, const double* __restrict__ stage, long long r0, long long nr, int mx,
-                                 int px, int xoff) {
+                                 int my, int mz, int px, int xoff, int nf, int pairs) {
   const long long total = nr * mx;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
     const long long r = q / mx;
     const int i = (int)(q - r * mx);
-    f[(r0 + r) * px + xoff - 3 + i] = (T)stage[q];
+    f[dev_index(r0 + r, i, my, mz, px, xoff, nf, pairs)] = (T)stage[q];
   }
 }
 
@@ -60,7 +76,7 @@ __global__ void load_rows_kernel(T* __restrict__ f, const double* __restrict__ s
 template <typename T>
 __global__ void store_rows_kernel(double* __restrict__ stage, const T* __restrict__ f, const T* __restrict__ carry,
                                   long long r0, long long nr, int nx, int ny, int nz, int px, int my, int mz,
-                                  int xoff) {
+                                  int xoff, int nf, int pairs) {
   const int mx = nx + 6;
   const long long total = nr * mx;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
@@ -68,15 +84,14 @@ __global__ void store_rows_kernel(double* __restrict__ stage, const T* __restric
     const long long r = q / mx;
     const int i = (int)(q - r * mx);
     const long long row = r0 + r;
-    double v = (double)f[row * px + xoff - 3 + i];
-    if (carry) {
+    double v = (double)f[dev_index(row, i, my, mz, px, xoff, nf, pairs)];
+    if (carry) {   // carry of the interior image of this (possibly ghost) cell
       const int j = (int)(row % my);
       long long rr = row / my;
       const int k = (int)(rr % mz);
       const long long fld = rr / mz;
-      const long long ci = fld * px * my * mz + (long long)(wrap(k, nz) + 3) * px * my + (long long)(wrap(j, ny) + 3) * px +
-                           xoff + wrap(i, nx);
-      v += (double)carry[ci];
+      const long long crow = (long long)(wrap(j, ny) + 3) + (long long)my * ((wrap(k, nz) + 3) + (long long)mz * fld);
+      v += (double)carry[dev_index(crow, wrap(i, nx) + 3, my, mz, px, xoff, nf, pairs)];
     }
     stage[q] = v;
   }
@@ -100,25 +115,26 @@ cudaError_t launch_ghost_fill(int tbytes, void* f, int nx, int ny, int nz, int p
   return cudaGetLastError();
 }
 
-cudaError_t launch_load_rows(int tbytes, void* f, const double* stage, long long r0, long long nr, int mx, int px,
-                             int xoff, cudaStream_t s) {
+cudaError_t launch_load_rows(int tbytes, void* f, const double* stage, long long r0, long long nr, int mx, int my,
+                             int mz, int px, int xoff, int nf, int pairs, cudaStream_t s) {
   const int th = 256, g = grid_for(nr * mx, th);
   if (tbytes == 4)
-    load_rows_kernel<float><<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, px, xoff);
+    load_rows_kernel<float><<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
   else
-    load_rows_kernel<double><<<g, th, 0, s>>>((double*)f, stage, r0, nr, mx, px, xoff);
+    load_rows_kernel<double><<<g, th, 0, s>>>((double*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
   return cudaGetLastError();
 }
 
 cudaError_t launch_store_rows(int tbytes, double* stage, const void* f, const void* carry, long long r0, long long nr,
-                              int nx, int ny, int nz, int px, int my, int mz, int xoff, cudaStream_t s) {
+                              int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs,
+                              cudaStream_t s) {
   const int th = 256, g = grid_for(nr * (nx + 6), th);
   if (tbytes == 4)
     store_rows_kernel<float><<<g, th, 0, s>>>(stage, (const float*)f, (const float*)carry, r0, nr, nx, ny, nz, px, my,
-                                              mz, xoff);
+                                              mz, xoff, nf, pairs);
   else
     store_rows_kernel<double><<<g, th, 0, s>>>(stage, (const double*)f, (const double*)carry, r0, nr, nx, ny, nz, px,
-                                               my, mz, xoff);
+                                               my, mz, xoff, nf, pairs);
   return cudaGetLastError();
 }
 
@@ -141,7 +157,7 @@ __device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
 template <typename T>
 __global__ void init_field_kernel(T* __restrict__ f, int kind, int comp, double ampl, double a, double b, double c,
                                   double k, unsigned long long seed, int nx, int ny, int nz, int px, int my, int xoff,
-                                  double x0, double y0, double z0, double dx, double dy, double dz) {
+                                  double x0, double y0, double z0, double dx, double dy, double dz, int estride) {
   const long long total = (long long)nx * ny * nz;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
@@ -149,7 +165,7 @@ __global__ void init_field_kernel(T* __restrict__ f, int kind, int comp, double 
     const long long r = q / nx;
     const int j = (int)(r % ny);
     const int kk = (int)(r / ny);
-    const long long idx = (long long)(kk + 3) * px * my + (long long)(j + 3) * px + xoff + i;
+    const long long idx = estride * ((long long)(kk + 3) * px * my + (long long)(j + 3) * px + xoff + i);
     if (kind == 0) {
       f[idx] = T(0);
     } else if (kind == 1) {
@@ -172,14 +188,15 @@ __global__ void init_field_kernel(T* __restrict__ f, int kind, int comp, double 
 
 cudaError_t launch_init_field(int tbytes, void* f, int kind, int comp, double ampl, double a, double b, double c,
                               double k, unsigned long long seed, int nx, int ny, int nz, int px, int my, int xoff,
-                              double x0, double y0, double z0, double dx, double dy, double dz, cudaStream_t s) {
+                              double x0, double y0, double z0, double dx, double dy, double dz, int estride,
+                              cudaStream_t s) {
   const int th = 256, g = grid_for((long long)nx * ny * nz, th);
   if (tbytes == 4)
     init_field_kernel<float><<<g, th, 0, s>>>((float*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my, xoff,
-                                              x0, y0, z0, dx, dy, dz);
+                                              x0, y0, z0, dx, dy, dz, estride);
   else
     init_field_kernel<double><<<g, th, 0, s>>>((double*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my,
-                                               xoff, x0, y0, z0, dx, dy, dz);
+                                               xoff, x0, y0, z0, dx, dy, dz, estride);
   return cudaGetLastError();
 }
 

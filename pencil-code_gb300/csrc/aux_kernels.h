@@ -5,13 +5,16 @@
 namespace pcgb {
 cudaError_t launch_ghost_fill(int tbytes, void* f, int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf,
                               cudaStream_t s);
-cudaError_t launch_load_rows(int tbytes, void* f, const double* stage, long long r0, long long nr, int mx, int px,
-                             int xoff, cudaStream_t s);
+// pairs = 1: packed field-pair layout (P0=(ux,ax) P1=(uy,ay) P2=(uz,az) P3=(lnrho,ss)), px/xoff in pair units
+cudaError_t launch_load_rows(int tbytes, void* f, const double* stage, long long r0, long long nr, int mx, int my,
+                             int mz, int px, int xoff, int nf, int pairs, cudaStream_t s);
 cudaError_t launch_store_rows(int tbytes, double* stage, const void* f, const void* carry, long long r0, long long nr,
-                              int nx, int ny, int nz, int px, int my, int mz, int xoff, cudaStream_t s);
+                              int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs,
+                              cudaStream_t s);
 }  // namespace pcgb
 namespace pcgb {
 cudaError_t launch_init_field(int tbytes, void* f, int kind, int comp, double ampl, double a, double b, double c,
                               double k, unsigned long long seed, int nx, int ny, int nz, int px, int my, int xoff,
-                              double x0, double y0, double z0, double dx, double dy, double dz, cudaStream_t s);
+                              double x0, double y0, double z0, double dx, double dy, double dz, int estride,
+                              cudaStream_t s);
 }  // namespace pcgb

@@ -1,0 +1,221 @@
+// cell_scalar.cuh -- cell policy with one value per field per cell (FP64, and
+// FP32 in the field-major layout).  Shared memory holds NF field slices per
+// plane; every stencil is a sequence of scalar loads.
+#pragma once
+
+#include "cell_physics.cuh"
+
+namespace pcgb {
+
+template <typename TT, int NF, int TX, int TY>
+struct ScalarCell {
+  using T = TT;
+  using Elem = TT;
+  static constexpr int NSLICE = NF;
+  static constexpr int BW = TX + 8, BH = TY + 6, FO = BW * BH;
+  static constexpr int IUX = 0, ILNRHO = 3, ISS = 4, IAX = NF - 3;
+  static constexpr bool ENTROPY = (NF == 8);
+
+  // Stencils on the 7 staged planes (each pointer at field 0, row ty+3, col tx+4).
+  struct St {
+    const T* const* pl;
+    const Fac<T>& F;
+    __device__ __forceinline__ T v(int dz, int k, int dy, int dx) const { return pl[dz + 3][k * FO + dy * BW + dx]; }
+    // der_main, deriv.f90:127-129 (x), :140-142 (y), :158-160 (z)
+    __device__ __forceinline__ T der(int k, int j) const {
+      if (j == 0)
+        return F.fx * ((T(45) * (v(0, k, 0, 1) - v(0, k, 0, -1)) - T(9) * (v(0, k, 0, 2) - v(0, k, 0, -2))) +
+                       (v(0, k, 0, 3) - v(0, k, 0, -3)));
+      if (j == 1)
+        return F.fy * ((T(45) * (v(0, k, 1, 0) - v(0, k, -1, 0)) - T(9) * (v(0, k, 2, 0) - v(0, k, -2, 0))) +
+                       (v(0, k, 3, 0) - v(0, k, -3, 0)));
+      return F.fz * ((T(45) * (v(1, k, 0, 0) - v(-1, k, 0, 0)) - T(9) * (v(2, k, 0, 0) - v(-2, k, 0, 0))) +
+                     (v(3, k, 0, 0) - v(-3, k, 0, 0)));
+    }
+    // der2_main 'standard', deriv.f90:39-41, :502-506
+    __device__ __forceinline__ T der2(int k, int j) const {
+      const T c0 = T(-490.0 / 180.0), c1 = T(270.0 / 180.0), c2 = T(-27.0 / 180.0), c3 = T(2.0 / 180.0);
+      const T f0 = v(0, k, 0, 0);
+      if (j == 0)
+        return F.sx * (((c0 * f0 + c1 * (v(0, k, 0, 1) + v(0, k, 0, -1))) + c2 * (v(0, k, 0, 2) + v(0, k, 0, -2))) +
+                       c3 * (v(0, k, 0, 3) + v(0, k, 0, -3)));
+      if (j == 1)
+        return F.sy * (((c0 * f0 + c1 * (v(0, k, 1, 0) + v(0, k, -1, 0))) + c2 * (v(0, k, 2, 0) + v(0, k, -2, 0))) +
+                       c3 * (v(0, k, 3, 0) + v(0, k, -3, 0)));
+      return F.sz * (((c0 * f0 + c1 * (v(1, k, 0, 0) + v(-1, k, 0, 0))) + c2 * (v(2, k, 0, 0) + v(-2, k, 0, 0))) +
+                     c3 * (v(3, k, 0, 0) + v(-3, k, 0, 0)));
+    }
+    // derij_main bidiagonal, deriv.f90:1387-1447; (a,b) with a<b: 0=x,1=y,2=z
+    __device__ __forceinline__ T derij(int k, int a, int b) const {
+      T t[3];
+#pragma unroll
+      for (int d = 1; d <= 3; ++d) {
+        if (a == 0 && b == 1)       // f(l+d,m+d) - f(l-d,m+d) + f(l-d,m-d) - f(l+d,m-d)
+          t[d - 1] = ((v(0, k, d, d) - v(0, k, d, -d)) + v(0, k, -d, -d)) - v(0, k, -d, d);
+        else if (a == 1 && b == 2)  // f(m+d,n+d) - f(m+d,n-d) + f(m-d,n-d) - f(m-d,n+d)
+          t[d - 1] = ((v(d, k, d, 0) - v(-d, k, d, 0)) + v(-d, k, -d, 0)) - v(d, k, -d, 0);
+        else                        // f(l+d,n+d) - f(l-d,n+d) + f(l-d,n-d) - f(l+d,n-d)
+          t[d - 1] = ((v(d, k, 0, d) - v(d, k, 0, -d)) + v(-d, k, 0, -d)) - v(-d, k, 0, d);
+      }
+      const T fac = (a == 0 && b == 1) ? F.mxy : ((a == 1 && b == 2) ? F.myz : F.mxz);
+      return fac * ((T(270) * t[0] - T(27) * t[1]) + T(2) * t[2]);
+    }
+  };
+
+  struct Tile {
+    Fac<T> F;
+    Phys<T> P;
+    T* fout;
+    T* dfp;
+    long long ps, fs;
+    int px, xoff, nx, ny, nz;
+    bool forcing, iso, vheat, oheat;
+    T fsx, fcx, fsy, fcy;
+    const T* sinz;
+    const T* cosz;
+    T dfnext[NF];
+
+    __device__ __forceinline__ void begin(const PcgbBoxDev& B, int inb, int x, int y, int z0, bool active,
+                                          bool mode_cfl, const StepFlags<T>& fl) {
+      make_fac(F, B);
+      make_phys(P, B);
+      fout = reinterpret_cast<T*>(B.f[inb ^ 1]);
+      dfp = reinterpret_cast<T*>(B.df);
+      ps = B.ps; fs = B.fs; px = B.px; xoff = B.xoff; nx = B.nx; ny = B.ny; nz = B.nz;
+      forcing = B.lforcing != 0; iso = B.isothermal != 0; vheat = B.lviscosity_heat != 0; oheat = B.lohmic_heat != 0;
+      const T* sinx = reinterpret_cast<const T*>(B.forc);
+      const T* cosx = sinx + B.px;
+      const T* siny = cosx + B.px;
+      const T* cosy = siny + B.my;
+      sinz = cosy + B.my;
+      cosz = sinz + B.mz;
+      fsx = fcx = fsy = fcy = T(0);
+      if (forcing && active) { fsx = sinx[x + 3]; fcx = cosx[x + 3]; fsy = siny[y + 3]; fcy = cosy[y + 3]; }
+#pragma unroll
+      for (int k = 0; k < NF; ++k) dfnext[k] = T(0);
+      if (fl.read_df && active && !mode_cfl) {
+        const long long c0 = (long long)(z0 + 3) * ps + (long long)(y + 3) * px + xoff + x;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) dfnext[k] = dfp[k * fs + c0];
+      }
+    }
+
+    __device__ __forceinline__ void step(const T* const pl[7], int x, int y, int z, int z1, const StepFlags<T>& fl,
+                                         Acc& acc, T& dt1max) {
+      const St st{pl, F};
+      const long long cidx = (long long)(z + 3) * ps + (long long)(y + 3) * px + xoff + x;
+      T dfo[NF];
+#pragma unroll
+      for (int k = 0; k < NF; ++k) dfo[k] = dfnext[k];
+      if (fl.read_df && z + 1 < z1) {
+#pragma unroll
+        for (int k = 0; k < NF; ++k) dfnext[k] = dfp[k * fs + cidx + ps];
+      }
+      CellIn<T> c;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        c.uu[i] = st.v(0, IUX + i, 0, 0);
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) c.uij[i][jj] = st.der(IUX + i, jj);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const T f0 = st.der2(IUX + i, 0), f1 = st.der2(IUX + i, 1), f2 = st.der2(IUX + i, 2);
+        c.del2u[i] = (f0 + f1) + f2;
+        // graddiv_i = sum_j d_i d_j u_j ; diagonal term from der2 (sub.f90:2646-2656)
+        const T g0 = (i == 0) ? f0 : st.derij(IUX + 0, 0, i);
+        const T g1 = (i == 1) ? f1 : st.derij(IUX + 1, 1 < i ? 1 : i, 1 < i ? i : 1);
+        const T g2 = (i == 2) ? f2 : st.derij(IUX + 2, i, 2);
+        c.graddivu[i] = (g0 + g1) + g2;
+      }
+      c.lnrho = st.v(0, ILNRHO, 0, 0);
+#pragma unroll
+      for (int jj = 0; jj < 3; ++jj) c.glnrho[jj] = st.der(ILNRHO, jj);
+      if (ENTROPY) {
+        c.ss = st.v(0, ISS, 0, 0);
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) c.gss[jj] = st.der(ISS, jj);
+        c.del2lnrho = (st.der2(ILNRHO, 0) + st.der2(ILNRHO, 1)) + st.der2(ILNRHO, 2);
+        c.del2ss = (st.der2(ISS, 0) + st.der2(ISS, 1)) + st.der2(ISS, 2);
+      } else {
+        c.ss = T(0); c.gss[0] = c.gss[1] = c.gss[2] = T(0); c.del2lnrho = c.del2ss = T(0);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        c.aa[i] = st.v(0, IAX + i, 0, 0);
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+          c.aij[i][jj] = st.der(IAX + i, jj);
+          c.a2[i][jj] = st.der2(IAX + i, jj);
+        }
+      }
+      c.a1xy = st.derij(IAX + 0, 0, 1); c.a2xy = st.derij(IAX + 1, 0, 1);
+      c.a1xz = st.derij(IAX + 0, 0, 2); c.a3xz = st.derij(IAX + 2, 0, 2);
+      c.a2yz = st.derij(IAX + 1, 1, 2); c.a3yz = st.derij(IAX + 2, 1, 2);
+      c.a3xy = c.a2xz = c.a1yz = T(0);
+      if (fl.want_diag) {
+        c.a3xy = st.derij(IAX + 2, 0, 1); c.a2xz = st.derij(IAX + 1, 0, 2); c.a1yz = st.derij(IAX + 0, 1, 2);
+      }
+      T fc[3] = {T(0), T(0), T(0)};
+      if (forcing) {   // forcing_cont 'ABC', forcing.f90:5894-5896
+        fc[0] = P.fact * (P.abc_c * sinz[z + 3] + (P.fact2 * P.abc_b) * fcy);
+        fc[1] = P.fact * (P.abc_a * fsx + (P.fact2 * P.abc_c) * cosz[z + 3]);
+        fc[2] = P.fact * (P.abc_b * fsy + (P.fact2 * P.abc_a) * fcx);
+      }
+      T dfn[NF];
+      cell_rhs<T, NF>(c, P, F, fc, forcing, iso, vheat, oheat, dfo, fl.alpha, dfn, fl.want_cfl, fl.want_diag, acc,
+                      dt1max);
+
+      // ---- 2N update (timestep.f90:160) and periodic ghost images ----
+      T fnew[NF], dsto[NF];
+#pragma unroll
+      for (int k = 0; k < NF; ++k) {
+        const T fc0 = st.v(0, k, 0, 0);
+        if (!fl.comp) {
+          fnew[k] = fc0 + fl.dtb * dfn[k];
+          dsto[k] = dfn[k];
+        } else {
+          // TwoSum of fc0 + y; on substep 1, y carries the previous step's compensation
+          const T yv = (fl.s == 0) ? (fl.dtb * dfn[k] + dfo[k]) : fl.dtb * dfn[k];
+          const T t = fc0 + yv;
+          const T bp = t - fc0;
+          const T e = (fc0 - (t - bp)) + (yv - bp);
+          fnew[k] = t;
+          dsto[k] = (fl.s < 2) ? (dfn[k] + e * fl.cinv) : e;
+        }
+      }
+      if (fl.write_df) {
+#pragma unroll
+        for (int k = 0; k < NF; ++k) dfp[k * fs + cidx] = dsto[k];
+      }
+#pragma unroll
+      for (int k = 0; k < NF; ++k) fout[k * fs + cidx] = fnew[k];
+      const bool edge = (x < 3) | (x >= nx - 3) | (y < 3) | (y >= ny - 3) | (z < 3) | (z >= nz - 3);
+      if (edge) {
+        const Images ix(x, nx), iy(y, ny), iz(z, nz);
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+              if ((a == 0 && b == 0 && e == 0) || a >= iz.n || b >= iy.n || e >= ix.n) continue;
+              const long long gi = (long long)(iz.v[a] + 3) * ps + (long long)(iy.v[b] + 3) * px + xoff + ix.v[e];
+#pragma unroll
+              for (int k = 0; k < NF; ++k) fout[k * fs + gi] = fnew[k];
+            }
+      }
+    }
+
+    __device__ __forceinline__ void cfl(const T* const pl[7], T& dt1max) {
+      const St st{pl, F};
+      const T uu[3] = {st.v(0, 0, 0, 0), st.v(0, 1, 0, 0), st.v(0, 2, 0, 0)};
+      const T bb[3] = {st.der(IAX + 2, 1) - st.der(IAX + 1, 2), st.der(IAX + 0, 2) - st.der(IAX + 2, 0),
+                       st.der(IAX + 1, 0) - st.der(IAX + 0, 1)};
+      const T d = cell_cfl_only<T, NF>(P, F, uu, st.v(0, ILNRHO, 0, 0), ENTROPY ? st.v(0, ISS, 0, 0) : T(0), bb, iso);
+      dt1max = (d > dt1max || d != d) ? d : dt1max;
+    }
+  };
+};
+
+}  // namespace pcgb

@@ -1,21 +1,27 @@
 // kernels.cuh -- host-side view of the compiled substep kernel variants.
 #pragma once
 #include <cuda_runtime.h>
-#include "mhd_substep.cuh"
+#include "cell_pair.cuh"
+#include "cell_scalar.cuh"
+#include "mhd_driver.cuh"
 
 namespace pcgb {
 
-// Tile variants (TX, TY).  The ring depth is fixed per precision.
+// Tile variants.  Ids 0..3 use the field-major layout (one value per field per
+// cell); for FP32, ids 4..7 use the packed field-pair layout (cell_pair.cuh).
+//   FP32: 0 (32,4)x2  1 (32,8)  2 (16,8)x2  3 (64,4)  4 pair(32,4)x2  5 pair(32,8)  6 pair(16,8)x2  7 pair(64,4)
+//   FP64: 0 (32,4)  1 (16,8)  2 (16,4)  3 (32,2)
+// "x2" variants ask for two resident CTAs per SM.
 struct TileShape { int tx, ty; };
-constexpr int kNumTiles = 4;
-// FP32 variants: (32,4) (32,8) (16,8) (64,4); FP64 variants: (32,4) (16,8) (16,4) (32,2).
-// FP32 (32,4) and (16,8) ask for two resident CTAs per SM.
+constexpr int kNumScalarTiles = 4;
+constexpr int kNumTiles = 8;
+inline int num_tiles(int dtype_bytes) { return dtype_bytes == 4 ? kNumTiles : kNumScalarTiles; }
+inline bool tile_is_pair(int dtype_bytes, int tile) { return dtype_bytes == 4 && tile >= kNumScalarTiles; }
 inline TileShape tile_shape(int dtype_bytes, int tile) {
-  static const TileShape f32[kNumTiles] = {{32, 4}, {32, 8}, {16, 8}, {64, 4}};
-  static const TileShape f64[kNumTiles] = {{32, 4}, {16, 8}, {16, 4}, {32, 2}};
-  return dtype_bytes == 4 ? f32[tile] : f64[tile];
+  static const TileShape f32[kNumScalarTiles] = {{32, 4}, {32, 8}, {16, 8}, {64, 4}};
+  static const TileShape f64[kNumScalarTiles] = {{32, 4}, {16, 8}, {16, 4}, {32, 2}};
+  return dtype_bytes == 4 ? f32[tile % kNumScalarTiles] : f64[tile];
 }
-constexpr int ring_depth(int dtype_bytes) { return dtype_bytes == 4 ? 9 : 8; }
 
 struct KernelHandle {
   const void* fn = nullptr;
@@ -34,44 +40,48 @@ inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile) {
   return nf == 8 ? kernel_f64_8(tile) : kernel_f64_7(tile);
 }
 
+template <class CELL, int TX, int TY, int R, int MB>
+static KernelHandle make_kernel_handle() {
+  KernelHandle h;
+  h.fn = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB>);
+  h.smem = DriverCfg<CELL, TX, TY, R>::SMEM_BYTES;
+  h.threads = TX * TY;
+  cudaFuncSetAttribute(&mhd_substep_kernel<CELL, TX, TY, R, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       h.smem);
+  return h;
+}
+
 }  // namespace pcgb
 
 // Instantiation helper used by the kernels_*.cu translation units.
-#define PCGB_DEFINE_KERNELS(NAME, T, NF)                                                   \
-  namespace pcgb {                                                                         \
-  template <int TX, int TY, int MB>                                                        \
-  static KernelHandle make_##NAME() {                                                      \
-    constexpr int R = ring_depth(sizeof(T));                                               \
-    KernelHandle h;                                                                        \
-    h.fn = reinterpret_cast<const void*>(&mhd_substep_kernel<T, NF, TX, TY, R, MB>);       \
-    h.smem = TileCfg<T, NF, TX, TY, R>::SMEM_BYTES;                                        \
-    h.threads = TX * TY;                                                                   \
-    cudaFuncSetAttribute(&mhd_substep_kernel<T, NF, TX, TY, R, MB>,                        \
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, h.smem);             \
-    return h;                                                                              \
-  }                                                                                        \
-  KernelHandle NAME(int tile) {                                                            \
-    static KernelHandle cache[kNumTiles];                                                  \
-    static bool init[kNumTiles] = {false, false, false, false};                            \
-    if (tile < 0 || tile >= kNumTiles) return KernelHandle();                              \
-    if (!init[tile]) {                                                                     \
-      if constexpr (sizeof(T) == 4) {                                                      \
-        switch (tile) {                                                                    \
-          case 0: cache[0] = make_##NAME<32, 4, 2>(); break;                               \
-          case 1: cache[1] = make_##NAME<32, 8, 1>(); break;                               \
-          case 2: cache[2] = make_##NAME<16, 8, 2>(); break;                               \
-          default: cache[3] = make_##NAME<64, 4, 1>(); break;                              \
-        }                                                                                  \
-      } else {                                                                             \
-        switch (tile) {                                                                    \
-          case 0: cache[0] = make_##NAME<32, 4, 1>(); break;                               \
-          case 1: cache[1] = make_##NAME<16, 8, 1>(); break;                               \
-          case 2: cache[2] = make_##NAME<16, 4, 1>(); break;                               \
-          default: cache[3] = make_##NAME<32, 2, 1>(); break;                              \
-        }                                                                                  \
-      }                                                                                    \
-      init[tile] = true;                                                                   \
-    }                                                                                      \
-    return cache[tile];                                                                    \
-  }                                                                                        \
+#define PCGB_DEFINE_KERNELS(NAME, T, NF)                                                           \
+  namespace pcgb {                                                                                 \
+  KernelHandle NAME(int tile) {                                                                    \
+    static KernelHandle cache[kNumTiles];                                                          \
+    static bool init[kNumTiles] = {false, false, false, false, false, false, false, false};        \
+    if (tile < 0 || tile >= num_tiles(sizeof(T))) return KernelHandle();                           \
+    if (!init[tile]) {                                                                             \
+      if constexpr (sizeof(T) == 4) {                                                              \
+        switch (tile) {                                                                            \
+          case 0: cache[0] = make_kernel_handle<ScalarCell<T, NF, 32, 4>, 32, 4, 9, 2>(); break;   \
+          case 1: cache[1] = make_kernel_handle<ScalarCell<T, NF, 32, 8>, 32, 8, 9, 1>(); break;   \
+          case 2: cache[2] = make_kernel_handle<ScalarCell<T, NF, 16, 8>, 16, 8, 9, 2>(); break;   \
+          case 3: cache[3] = make_kernel_handle<ScalarCell<T, NF, 64, 4>, 64, 4, 9, 1>(); break;   \
+          case 4: cache[4] = make_kernel_handle<PairCell<NF, 32, 4>, 32, 4, 8, 2>(); break;        \
+          case 5: cache[5] = make_kernel_handle<PairCell<NF, 32, 8>, 32, 8, 9, 1>(); break;        \
+          case 6: cache[6] = make_kernel_handle<PairCell<NF, 16, 8>, 16, 8, 8, 2>(); break;        \
+          default: cache[7] = make_kernel_handle<PairCell<NF, 64, 4>, 64, 4, 8, 1>(); break;       \
+        }                                                                                          \
+      } else {                                                                                     \
+        switch (tile) {                                                                            \
+          case 0: cache[0] = make_kernel_handle<ScalarCell<T, NF, 32, 4>, 32, 4, 8, 1>(); break;   \
+          case 1: cache[1] = make_kernel_handle<ScalarCell<T, NF, 16, 8>, 16, 8, 8, 1>(); break;   \
+          case 2: cache[2] = make_kernel_handle<ScalarCell<T, NF, 16, 4>, 16, 4, 8, 1>(); break;   \
+          default: cache[3] = make_kernel_handle<ScalarCell<T, NF, 32, 2>, 32, 2, 8, 1>(); break;  \
+        }                                                                                          \
+      }                                                                                            \
+      init[tile] = true;                                                                           \
+    }                                                                                              \
+    return cache[tile];                                                                            \
+  }                                                                                                \
   }

@@ -1,0 +1,142 @@
+// mhd_common.cuh -- pieces shared by the substep kernel's cell policies.
+#pragma once
+
+#include <math.h>
+#include "pcgb_box.h"
+#include "pcgb_ptx.cuh"
+
+namespace pcgb {
+
+enum { MODE_SUBSTEP = 0, MODE_CFL = 1 };
+
+struct LaunchArgs {
+  const PcgbBoxDev* boxes;    // [nboxes], sorted by tile0
+  int nboxes;
+  int total_tiles;            // sum of boxes[b].tiles
+  unsigned int* work_counter; // non-null: persistent CTAs pull tiles from this counter
+  int mode;                   // MODE_SUBSTEP or MODE_CFL
+  unsigned int wait_limit;    // bounded mbarrier wait (iterations)
+};
+
+// Williamson (1980) low-storage RK3, timestep.f90:43-44.
+__device__ __forceinline__ double rk_alpha(int s) { return s == 0 ? 0.0 : (s == 1 ? -5.0 / 9.0 : -153.0 / 128.0); }
+__device__ __forceinline__ double rk_beta(int s) { return s == 0 ? 1.0 / 3.0 : (s == 1 ? 15.0 / 16.0 : 8.0 / 15.0); }
+
+__device__ __forceinline__ float texp(float v) { return expf(v); }
+__device__ __forceinline__ double texp(double v) { return exp(v); }
+__device__ __forceinline__ float tsqrt(float v) { return sqrtf(v); }
+__device__ __forceinline__ double tsqrt(double v) { return sqrt(v); }
+__device__ __forceinline__ float tabs(float v) { return fabsf(v); }
+__device__ __forceinline__ double tabs(double v) { return fabs(v); }
+
+// Stencil factors and grid constants in the arithmetic type.
+template <typename T>
+struct Fac {
+  T fx, fy, fz;        // (1/60)*dx_1 ...            deriv.f90:127
+  T sx, sy, sz;        // dx_1**2 ...                deriv.f90:502
+  T mxy, myz, mxz;     // (1/720)*dx_1*dy_1 ...      deriv.f90:1392,1408,1424
+  T dx1, dy1, dz1, dxyz2;
+};
+
+// Physics constants of one box in type T.
+template <typename T>
+struct Phys {
+  T nu, eta, chi_cp, mu0, mu01, cs20, gamma_m1, gamma1, lnrho0, cv1, lnTT0, two_nu, eta_mu0, gamma_chi;
+  T bx, by, bz, fact, fact2, abc_a, abc_b, abc_c, ampl_fc, cdt1, cdtv1;
+  T maxdiffus;   // max(diffus_nu, diffus_eta, diffus_chi): constant in space for this physics
+};
+
+template <typename T>
+__device__ __forceinline__ void make_fac(Fac<T>& F, const PcgbBoxDev& B) {
+  F.dx1 = T(B.dx_1); F.dy1 = T(B.dy_1); F.dz1 = T(B.dz_1); F.dxyz2 = T(B.dxyz_2);
+  F.fx = T((1.0 / 60.0) * B.dx_1); F.fy = T((1.0 / 60.0) * B.dy_1); F.fz = T((1.0 / 60.0) * B.dz_1);
+  F.sx = T(B.dx_1 * B.dx_1); F.sy = T(B.dy_1 * B.dy_1); F.sz = T(B.dz_1 * B.dz_1);
+  F.mxy = T(((1.0 / 720.0) * B.dx_1) * B.dy_1);
+  F.myz = T(((1.0 / 720.0) * B.dy_1) * B.dz_1);
+  F.mxz = T(((1.0 / 720.0) * B.dz_1) * B.dx_1);
+}
+
+template <typename T>
+__device__ __forceinline__ void make_phys(Phys<T>& P, const PcgbBoxDev& B) {
+  P.nu = T(B.nu); P.eta = T(B.eta); P.chi_cp = T(B.chi * B.cpp); P.mu0 = T(B.mu0); P.mu01 = T(B.mu01);
+  P.cs20 = T(B.cs20); P.gamma_m1 = T(B.gamma_m1); P.gamma1 = T(B.gamma1); P.lnrho0 = T(B.lnrho0);
+  P.cv1 = T(B.cv1); P.lnTT0 = T(B.lnTT0); P.two_nu = T(2.0 * B.nu); P.eta_mu0 = T(B.eta * B.mu0);
+  P.gamma_chi = T(B.gamma * B.chi);
+  P.bx = T(B.b_ext[0]); P.by = T(B.b_ext[1]); P.bz = T(B.b_ext[2]);
+  P.fact = T(B.fact); P.fact2 = T(B.fact2); P.abc_a = T(B.abc_a); P.abc_b = T(B.abc_b); P.abc_c = T(B.abc_c);
+  P.ampl_fc = T(B.ampl_fcont_uu); P.cdt1 = T(1.0 / B.cdt); P.cdtv1 = T(1.0 / B.cdtv);
+  // viscosity.f90:2436, magnetic.f90:6541, entropy.f90:4905
+  double mdiff = B.nu * B.dxyz_2;
+  if (B.eta * B.dxyz_2 > mdiff) mdiff = B.eta * B.dxyz_2;
+  if (B.lentropy && (B.gamma * B.chi) * B.dxyz_2 > mdiff) mdiff = (B.gamma * B.chi) * B.dxyz_2;
+  P.maxdiffus = T(mdiff);
+}
+
+// Per-thread FP64 reduction accumulators.
+struct Acc {
+  double v[PCGB_NSLOT];
+  __device__ __forceinline__ void reset() {
+#pragma unroll
+    for (int i = 0; i < PCGB_NSLOT; ++i) v[i] = 0.0;
+  }
+};
+
+__device__ __forceinline__ bool slot_is_max(int s) {
+  return s == PCGB_S_DT1MAX || s == PCGB_S_U2MAX || s == PCGB_S_B2MAX;
+}
+
+__device__ __forceinline__ double red_op(int q, double a, double b) {
+  return slot_is_max(q) ? ((b > a || b != b) ? b : a) : a + b;
+}
+
+// CFL inverse timestep of one cell, set_dt1_max (equ.f90:1872-1905), with
+// maxadvec/maxdiffus as assembled by hydro.f90:3500, magnetic.f90:5180,
+// noentropy.f90:316 / entropy.f90:3640.
+template <typename T>
+__device__ __forceinline__ T cfl_dt1(const Phys<T>& P, const Fac<T>& F, const T u[3], const T bb[3], T rho1, T cs2) {
+  T advec_uu = (tabs(u[0]) * F.dx1 + tabs(u[1]) * F.dy1) + tabs(u[2]) * F.dz1;
+  T maxadvec = advec_uu > T(0) ? advec_uu : T(0);
+  T t0 = bb[0] * F.dx1, t1 = bb[1] * F.dy1, t2 = bb[2] * F.dz1;
+  T advec_va2 = (((t0 * t0 + t1 * t1) + t2 * t2) * P.mu01) * rho1;
+  T advec_cs2 = cs2 * F.dxyz2;
+  maxadvec = maxadvec + tsqrt((T(0) + advec_va2) + advec_cs2);
+  T a = maxadvec * P.cdt1, d = P.maxdiffus * P.cdtv1;
+  return tsqrt(a * a + d * d);
+}
+
+// Everything a cell needs to know about the current substep.
+template <typename T>
+struct StepFlags {
+  int s;            // substep 0..2
+  T alpha, dtb;     // alpha_s, dt*beta_s
+  T cinv;           // 1/(dt*beta_{s+1}*alpha_{s+1}) for the compensated carry
+  bool comp, read_df, write_df, want_cfl, want_diag;
+};
+
+// Periodic images of an interior index: the index itself and, near a face,
+// its copy in the ghost zone on the opposite side (boundcond.f90:2387-2531).
+struct Images {
+  int v[2];
+  int n;
+  __device__ __forceinline__ Images(int i, int nn) {
+    v[0] = i; n = 1;
+    if (i < 3) v[n++] = i + nn;
+    else if (i >= nn - 3) v[n++] = i - nn;
+  }
+};
+
+// Diagnostic accumulation (FP64) of one cell.
+__device__ __forceinline__ void acc_diag(Acc& acc, double u2, double b2, double lnrho, double divb, double j2, double ab) {
+  const double rho = exp(lnrho);
+  acc.v[PCGB_S_U2SUM] += u2;
+  acc.v[PCGB_S_U2MAX] = fmax(acc.v[PCGB_S_U2MAX], u2);
+  acc.v[PCGB_S_B2SUM] += b2;
+  acc.v[PCGB_S_B2MAX] = fmax(acc.v[PCGB_S_B2MAX], b2);
+  acc.v[PCGB_S_EKINSUM] += 0.5 * rho * u2;
+  acc.v[PCGB_S_RHOSUM] += rho;
+  acc.v[PCGB_S_DIVB2SUM] += divb * divb;
+  acc.v[PCGB_S_J2SUM] += j2;
+  acc.v[PCGB_S_ABSUM] += ab;
+}
+
+}  // namespace pcgb

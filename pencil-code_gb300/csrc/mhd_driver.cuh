@@ -1,0 +1,272 @@
+// mhd_driver.cuh -- the fused RK substep kernel (sm_103a): work distribution,
+// TMA plane ring, reductions and step bookkeeping, generic over a cell policy.
+//
+// One launch advances every box of a batch by one 2N-RK3 substep
+// (timestep.f90:77-202).  The cell policy evaluates, for one output cell,
+// the compressible-MHD right-hand side of pde() (equ.f90:1386 rhs_cpu: duu_dt,
+// dlnrho_dt, denergy_dt, daa_dt) with the 6th-order der/der2/bidiagonal derij
+// stencils (deriv.f90:89,472,1367), applies df = alpha*df + RHS and
+// f_out = f_in + dt*beta*df, and writes f_out's periodic ghost images
+// (boundcond.f90:2387-2531) in the same pass.
+//
+// Work decomposition: a tile is TX x TY columns of one box swept over zd
+// z-planes.  Every field slice of one ghosted plane (TX+8) x (TY+6) is staged
+// into a ring of RING shared-memory slots by one 4-D TMA load per plane,
+// tracked by one mbarrier per slot; output plane z reads planes z-3..z+3.
+// Work items come from blockIdx (one tile per CTA) or, for persistent batched
+// launches, from an atomic tile counter.
+//
+// Reductions (CFL inverse timestep and diagnostics) are accumulated in FP64,
+// written per tile, and reduced in fixed tile order by the last CTA of each
+// box, which also advances the box's bookkeeping (substep index, time, dt)
+// in device memory, so a time loop is a sequence of identical launches.
+#pragma once
+
+#include "mhd_common.cuh"
+
+namespace pcgb {
+
+template <class CELL, int TX, int TY, int RING>
+struct DriverCfg {
+  using Elem = typename CELL::Elem;
+  static constexpr int NT = TX * TY;
+  static constexpr int NWARP = (NT + 31) / 32;
+  static constexpr int BW = TX + 8;   // TMA box width: x0-4 .. x0+TX+4
+  static constexpr int BH = TY + 6;   // TMA box rows:  y0-3 .. y0+TY+3
+  static constexpr int PLANE_BYTES = CELL::NSLICE * BW * BH * (int)sizeof(Elem);
+  static constexpr int SLOT_BYTES = (PLANE_BYTES + 127) / 128 * 128;
+  static constexpr int RED_OFF = RING * SLOT_BYTES + RING * 8;
+  static constexpr int SMEM_BYTES = RED_OFF + NWARP * PCGB_NSLOT * 8 + 64;
+};
+
+template <class CELL, int TX, int TY, int RING, int MINB>
+__global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs args) {
+  using C = DriverCfg<CELL, TX, TY, RING>;
+  using T = typename CELL::T;
+  using Elem = typename CELL::Elem;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + RING * C::SLOT_BYTES);
+  double* red = reinterpret_cast<double*>(smem + C::RED_OFF);
+  int* sh = reinterpret_cast<int*>(smem + C::RED_OFF + C::NWARP * PCGB_NSLOT * 8);
+
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+  const int lane = tid & 31, warp = tid >> 5;
+
+  if (tid == 0) {
+    for (int r = 0; r < RING; ++r) mbar_init(&full[r], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  unsigned long long gplane = 0;   // planes loaded by this CTA so far (ring phase tracking)
+  int iter = 0;
+  int failed = 0;
+
+  while (true) {
+    int w;
+    if (args.work_counter) {
+      if (tid == 0) sh[0] = (int)atomicAdd(args.work_counter, 1u);
+      __syncthreads();
+      w = sh[0];
+      __syncthreads();
+    } else {
+      w = (iter == 0) ? (int)blockIdx.x : args.total_tiles;
+    }
+    ++iter;
+    if (w >= args.total_tiles) break;
+
+    // locate the box of work item w (binary search over tile0)
+    int lo = 0, hi = args.nboxes - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (args.boxes[mid].tile0 <= w) lo = mid; else hi = mid - 1;
+    }
+    const PcgbBoxDev& B = args.boxes[lo];
+    PcgbBoxState* S = B.state;
+
+    const int lt = w - B.tile0;
+    const int ntx = B.ntx, nty = B.nty;
+    const int tix = lt % ntx, tiy = (lt / ntx) % nty, tiz = lt / (ntx * nty);
+    const int x0 = tix * TX, y0 = tiy * TY, z0 = tiz * B.zd;
+    const int z1 = min(z0 + B.zd, B.nz);
+    const int nplanes = (z1 - z0) + 6;
+
+    const unsigned long long nsub = __ldcg(&S->nsub);
+    const int s = (int)(nsub % 3ull);
+    const int inb = (int)(nsub & 1ull);
+    const CUtensorMap* tmap = &B.tmap[inb];
+    const double dt = __ldcg(&S->dt);
+    const bool mode_cfl = (args.mode == MODE_CFL);
+    const unsigned long long step = nsub / 3ull + __ldcg(&S->step0);
+    StepFlags<T> fl;
+    fl.s = s;
+    fl.want_diag = !mode_cfl && s == 0 &&
+                   ((B.diag_every > 0 && (step % (unsigned long long)B.diag_every) == 0ull) ||
+                    __ldcg(&S->diag_request) != 0);
+    fl.want_cfl = mode_cfl || (s == 0 && B.dt_mode == PCGB_DT_LAGGED);
+    fl.comp = (B.comp != 0);
+    fl.read_df = (s > 0) || fl.comp;
+    fl.write_df = (s < 2) || fl.comp;
+    fl.alpha = T(rk_alpha(s));
+    fl.dtb = T(dt * rk_beta(s));
+    // compensated mode: df_stored = df + e / (dt*beta_{s+1}*alpha_{s+1})
+    fl.cinv = (fl.comp && s < 2) ? T(1.0 / (dt * rk_beta(s + 1) * rk_alpha(s + 1))) : T(0);
+    const bool need_red = fl.want_cfl || fl.want_diag;
+
+    // producer: prologue
+    if (tid == 0) {
+      prefetch_tensormap(tmap);
+      const int npro = nplanes < RING ? nplanes : RING;
+      for (int j = 0; j < npro; ++j) {
+        const unsigned long long G = gplane + (unsigned long long)j;
+        const int slot = (int)(G % RING);
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&full[slot], C::PLANE_BYTES);
+        tma_load_4d(smem + slot * C::SLOT_BYTES, tmap, &full[slot], B.xoff + x0 - 4, y0, z0 + j, 0);
+      }
+    }
+
+    const int x = x0 + tx, y = y0 + ty;
+    const bool active = (x < B.nx) && (y < B.ny);
+    typename CELL::Tile cell;
+    cell.begin(B, inb, x, y, z0, active, mode_cfl, fl);
+
+    Acc acc;
+    acc.reset();
+    T dt1max = T(0);
+
+    for (int z = z0; z < z1; ++z) {
+      const int j = z - z0;
+      // wait for planes j..j+6 (only the newest is new after the first plane)
+      const int jw0 = (j == 0) ? 0 : j + 6;
+      int lfail = 0;
+      for (int jw = jw0; jw <= j + 6; ++jw) {
+        const unsigned long long G = gplane + (unsigned long long)jw;
+        if (!mbar_wait_bounded(&full[G % RING], (uint32_t)((G / RING) & 1ull), args.wait_limit)) lfail = 1;
+      }
+      if (__syncthreads_or(lfail)) {
+        failed = 1;
+        // drain: wait (bounded) for every plane still in flight before leaving
+        if (tid == 0) {
+          const int hi2 = (j + RING < nplanes) ? j + RING : nplanes;
+          for (int jw = j; jw < hi2; ++jw) {
+            const unsigned long long G = gplane + (unsigned long long)jw;
+            mbar_wait_bounded(&full[G % RING], (uint32_t)((G / RING) & 1ull), args.wait_limit);
+          }
+        }
+        break;
+      }
+
+      if (active) {
+        const Elem* pl[7];
+#pragma unroll
+        for (int d = 0; d < 7; ++d) {
+          const unsigned long long G = gplane + (unsigned long long)(j + d);
+          pl[d] = reinterpret_cast<const Elem*>(smem + (G % RING) * C::SLOT_BYTES) + (ty + 3) * C::BW + (tx + 4);
+        }
+        if (!mode_cfl) cell.step(pl, x, y, z, z1, fl, acc, dt1max);
+        else cell.cfl(pl, dt1max);
+      }
+
+      __syncthreads();   // every thread is done with plane j
+      if (tid == 0 && j + RING < nplanes) {
+        const unsigned long long G = gplane + (unsigned long long)(j + RING);
+        const int slot = (int)(G % RING);
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&full[slot], C::PLANE_BYTES);
+        tma_load_4d(smem + slot * C::SLOT_BYTES, tmap, &full[slot], B.xoff + x0 - 4, y0, z0 + j + RING, 0);
+      }
+    }
+    gplane += (unsigned long long)nplanes;
+    if (failed) {
+      if (tid == 0) atomicOr(&S->err, PCGB_ERR_TIMEOUT);
+      break;
+    }
+
+    // ---- per-tile reduction (fixed order: lanes, then warps) ----
+    if (need_red) {
+      acc.v[PCGB_S_DT1MAX] = (double)dt1max;
+#pragma unroll
+      for (int q = 0; q < PCGB_NSLOT; ++q) {
+        double vq = acc.v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) vq = red_op(q, vq, __shfl_xor_sync(0xffffffffu, vq, o));
+        if (lane == 0) red[warp * PCGB_NSLOT + q] = vq;
+      }
+      __syncthreads();
+      if (tid < PCGB_NSLOT) {
+        double r = red[tid];
+        for (int wq = 1; wq < C::NWARP; ++wq) r = red_op(tid, r, red[wq * PCGB_NSLOT + tid]);
+        B.partial[(long long)lt * PCGB_NSLOT + tid] = r;
+      }
+    }
+
+    // ---- last CTA of the box: reduce tiles in order, advance bookkeeping ----
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+      const unsigned int prev = atomicAdd(&S->done, 1u);
+      sh[1] = (prev == (unsigned int)(B.tiles - 1)) ? 1 : 0;
+    }
+    __syncthreads();
+    if (sh[1]) {
+      __threadfence();
+      if (need_red) {
+        double part[PCGB_NSLOT];
+#pragma unroll
+        for (int q = 0; q < PCGB_NSLOT; ++q) part[q] = 0.0;
+        for (int t = tid; t < B.tiles; t += C::NT) {
+#pragma unroll
+          for (int q = 0; q < PCGB_NSLOT; ++q)
+            part[q] = red_op(q, part[q], __ldcg(&B.partial[(long long)t * PCGB_NSLOT + q]));
+        }
+#pragma unroll
+        for (int q = 0; q < PCGB_NSLOT; ++q) {
+          double vq = part[q];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) vq = red_op(q, vq, __shfl_xor_sync(0xffffffffu, vq, o));
+          if (lane == 0) red[warp * PCGB_NSLOT + q] = vq;
+        }
+        __syncthreads();
+        if (tid == 0) {
+          double r[PCGB_NSLOT];
+          for (int q = 0; q < PCGB_NSLOT; ++q) {
+            r[q] = red[q];
+            for (int wq = 1; wq < C::NWARP; ++wq) r[q] = red_op(q, r[q], red[wq * PCGB_NSLOT + q]);
+          }
+          if (fl.want_cfl) {
+            const double dtn = 1.0 / r[PCGB_S_DT1MAX];   // set_dt, sub.f90:4247
+            if (!(dtn > 0.0) || !isfinite(dtn)) atomicOr(&S->err, PCGB_ERR_DT | PCGB_ERR_NONFINITE);
+            if (mode_cfl) {
+              if (B.dt_mode != PCGB_DT_FIXED) { S->dt = dtn; S->dt_next = dtn; }
+            } else {
+              S->dt_next = dtn;
+            }
+          }
+          if (fl.want_diag) {
+            for (int q = 0; q < PCGB_NSLOT; ++q) S->diag[q] = r[q];
+            S->diag_step = step;
+            S->diag_request = 0;
+          }
+        }
+      }
+      if (tid == 0) {
+        if (!mode_cfl) {
+          // ds and time bookkeeping, timestep.f90:108-148, :201
+          double ds = (s == 0) ? 0.0 : rk_alpha(s) * S->ds;
+          ds = ds + 1.0;
+          S->ds = ds;
+          S->t = S->t + ds * (dt * rk_beta(s));
+          if (s == 2 && B.dt_mode == PCGB_DT_LAGGED) S->dt = S->dt_next;
+          S->nsub = nsub + 1ull;
+        }
+        S->done = 0u;
+        __threadfence();
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace pcgb

@@ -98,7 +98,8 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
   const int px = xoff + ((p->nx + 8 + xoff - 1) / xoff) * xoff;
   const int my = p->ny + 6, mz = p->nz + 6, mx = p->nx + 6;
   const int tile = p->tile >= 0 ? p->tile : 0;
-  if (tile >= kNumTiles) return fail(2, "tile variant out of range");
+  // the documented layout is field-major: only the field-major tile variants apply
+  if (tile >= kNumScalarTiles) return fail(2, "tile variant out of range");
   const TileShape ts = tile_shape(tb, tile);
   const KernelHandle kh = get_kernel(tb, nf, tile);
   if (!kh.fn) return fail(2, "no kernel for this tile variant");

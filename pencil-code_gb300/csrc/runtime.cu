@@ -118,6 +118,9 @@ static int engine_init() {
 struct pcgb_box {
   pcgb_params p;
   int nf = 7, tb = 8, tile = 0, zd = 0, tx = 32, ty = 4;
+  int pairs = 0;   // packed field-pair layout (FP32 tiles 4..7)
+  int eb = 8;      // bytes per device element (T, or float2 with pairs)
+  int ns = 7;      // slices per plane (nf, or 4 pairs)
   int nx = 0, ny = 0, nz = 0, mx = 0, my = 0, mz = 0, px = 0, xoff = 0;
   long long ps = 0, fs = 0;
   size_t fbytes = 0;    // bytes of one f buffer
@@ -188,11 +191,12 @@ static int upload_forcing(pcgb_box* b) {
 
 static int encode_maps(pcgb_box* b) {
   for (int q = 0; q < 2; ++q) {
-    cuuint64_t dims[4] = {(cuuint64_t)b->px, (cuuint64_t)b->my, (cuuint64_t)b->mz, (cuuint64_t)b->nf};
-    cuuint64_t strides[3] = {(cuuint64_t)b->px * b->tb, (cuuint64_t)b->ps * b->tb, (cuuint64_t)b->fs * b->tb};
-    cuuint32_t box[4] = {(cuuint32_t)(b->tx + 8), (cuuint32_t)(b->ty + 6), 1u, (cuuint32_t)b->nf};
+    cuuint64_t dims[4] = {(cuuint64_t)b->px, (cuuint64_t)b->my, (cuuint64_t)b->mz, (cuuint64_t)b->ns};
+    cuuint64_t strides[3] = {(cuuint64_t)b->px * b->eb, (cuuint64_t)b->ps * b->eb, (cuuint64_t)b->fs * b->eb};
+    cuuint32_t box[4] = {(cuuint32_t)(b->tx + 8), (cuuint32_t)(b->ty + 6), 1u, (cuuint32_t)b->ns};
     cuuint32_t es[4] = {1, 1, 1, 1};
-    CUresult r = g.encode(&b->hdev.tmap[q], b->tb == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+    // TMA moves bytes: a float2 pair travels as one 8-byte element
+    CUresult r = g.encode(&b->hdev.tmap[q], b->eb == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
                           4, b->f[q], dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -209,9 +213,13 @@ static int default_zdepth(const pcgb_box* b) {
   return zd;
 }
 
+static int default_tile(int tb) { return tb == 4 ? 4 : 0; }
+
 static int set_tiling(pcgb_box* b, int tile, int zd) {
-  if (tile < 0) tile = (b->tb == 4) ? 1 : 0;
-  if (tile >= kNumTiles) return set_err(PCGB_E_ARG, "tile variant %d out of range", tile);
+  if (tile < 0) tile = default_tile(b->tb);
+  if (tile >= num_tiles(b->tb)) return set_err(PCGB_E_ARG, "tile variant %d out of range", tile);
+  if ((int)tile_is_pair(b->tb, tile) != b->pairs)
+    return set_err(PCGB_E_ARG, "tile %d needs a different device layout than this box was created with", tile);
   TileShape ts = tile_shape(b->tb, tile);
   KernelHandle kh = get_kernel(b->tb, b->nf, tile);
   if (!kh.fn) return set_err(PCGB_E_ARG, "no kernel for tile %d", tile);
@@ -264,11 +272,17 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   b->tb = p->precision;
   b->nx = p->nx; b->ny = p->ny; b->nz = p->nz;
   b->mx = p->nx + 6; b->my = p->ny + 6; b->mz = p->nz + 6;
-  b->xoff = 128 / b->tb;
+  {
+    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb);
+    b->pairs = (t0 < num_tiles(b->tb) && tile_is_pair(b->tb, t0)) ? 1 : 0;
+  }
+  b->eb = b->pairs ? 8 : b->tb;
+  b->ns = b->pairs ? 4 : b->nf;
+  b->xoff = 128 / b->eb;
   b->px = b->xoff + ((b->nx + 8 + b->xoff - 1) / b->xoff) * b->xoff;
   b->ps = (long long)b->px * b->my;
   b->fs = b->ps * b->mz;
-  b->fbytes = (size_t)b->fs * b->nf * b->tb;
+  b->fbytes = (size_t)b->fs * b->ns * b->eb;
   memset(&b->hdev, 0, sizeof(b->hdev));
   auto fail = [&](const char* what) {
     set_err(PCGB_E_NOMEM, "device allocation of %s failed (%zu bytes per f buffer)", what, b->fbytes);
@@ -313,8 +327,8 @@ extern "C" size_t pcgb_box_bytes(const pcgb_box* b) {
 
 extern "C" int pcgb_box_info(const pcgb_box* b, int* info, int ninfo) {
   if (!b || !info) return set_err(PCGB_E_ARG, "null argument");
-  int v[10] = {b->nx, b->ny, b->nz, b->nf, b->tb, b->tile, b->zd, b->tiles, b->px, b->xoff};
-  for (int i = 0; i < ninfo && i < 10; ++i) info[i] = v[i];
+  int v[11] = {b->nx, b->ny, b->nz, b->nf, b->tb, b->tile, b->zd, b->tiles, b->px, b->xoff, b->pairs};
+  for (int i = 0; i < ninfo && i < 11; ++i) info[i] = v[i];
   return 0;
 }
 
@@ -363,7 +377,7 @@ static int box_check_state(pcgb_box* b) {
 // FP32 carry), restart the step bookkeeping at substep 1 with time t.
 static int box_reset(pcgb_box* b, double t) {
   const int in = cur_in(b);
-  CK(launch_ghost_fill(b->tb, b->f[in], b->nx, b->ny, b->nz, b->px, b->my, b->mz, b->xoff, b->nf, g.stream));
+  CK(launch_ghost_fill(b->eb, b->f[in], b->nx, b->ny, b->nz, b->px, b->my, b->mz, b->xoff, b->ns, g.stream));
   ++g.launches;
   CK(cudaMemsetAsync(b->df, 0, b->fbytes, g.stream));
   PcgbBoxState st;
@@ -392,7 +406,8 @@ extern "C" int pcgb_box_load(pcgb_box* b, const double* fh, double t) {
   for (long long r0 = 0; r0 < rows; r0 += chunk) {
     const long long nr = std::min(chunk, rows - r0);
     CK(cudaMemcpyAsync(g.stage, fh + r0 * b->mx, (size_t)(nr * b->mx) * sizeof(double), cudaMemcpyHostToDevice, g.stream));
-    CK(launch_load_rows(b->tb, b->f[in], g.stage, r0, nr, b->mx, b->px, b->xoff, g.stream));
+    CK(launch_load_rows(b->tb, b->f[in], g.stage, r0, nr, b->mx, b->my, b->mz, b->px, b->xoff, b->nf, b->pairs,
+                        g.stream));
     ++g.launches;
   }
   return box_reset(b, t);
@@ -406,11 +421,20 @@ extern "C" int pcgb_box_init_field(pcgb_box* b, int field, int kind, double ampl
   std::lock_guard<std::mutex> lk(g_mu);
   if (!b || field < 0 || field >= b->nf || kind < 0 || kind > 2) return set_err(PCGB_E_ARG, "bad argument");
   const int in = cur_in(b);
-  char* base = static_cast<char*>(b->f[in]) + (size_t)field * b->fs * b->tb;
+  // slice and lane of the field: field-major, or P0=(ux,ax) P1=(uy,ay) P2=(uz,az) P3=(lnrho,ss)
+  int slice = field, lane = 0;
+  if (b->pairs) {
+    const int iax = b->nf - 3;
+    if (field < 4) { slice = field; lane = 0; }
+    else if (b->nf == 8 && field == 4) { slice = 3; lane = 1; }
+    else { slice = field - iax; lane = 1; }
+  }
+  char* base = static_cast<char*>(b->f[in]) + (size_t)slice * b->fs * b->eb + (size_t)lane * b->tb;
   const pcgb_params& p = b->p;
-  CK(launch_init_field(b->tb, base, kind, kind == 2 ? field : 0, ampl, a, bb, c, k, seed, b->nx, b->ny, b->nz, b->px,
+  const int comp = (field < 3) ? field : 0;   // ABC component of uu
+  CK(launch_init_field(b->tb, base, kind, kind == 2 ? comp : 0, ampl, a, bb, c, k, seed, b->nx, b->ny, b->nz, b->px,
                        b->my, b->xoff, p.xyz0[0], p.xyz0[1], p.xyz0[2], p.Lxyz[0] / p.nx, p.Lxyz[1] / p.ny,
-                       p.Lxyz[2] / p.nz, g.stream));
+                       p.Lxyz[2] / p.nz, b->pairs ? 2 : 1, g.stream));
   ++g.launches;
   return box_reset(b, 0.0);
 }
@@ -426,7 +450,7 @@ extern "C" int pcgb_box_store(pcgb_box* b, double* fh) {
   for (long long r0 = 0; r0 < rows; r0 += chunk) {
     const long long nr = std::min(chunk, rows - r0);
     CK(launch_store_rows(b->tb, g.stage, b->f[in], carry, r0, nr, b->nx, b->ny, b->nz, b->px, b->my, b->mz, b->xoff,
-                         g.stream));
+                         b->nf, b->pairs, g.stream));
     ++g.launches;
     CK(cudaMemcpyAsync(fh + r0 * b->mx, g.stage, (size_t)(nr * b->mx) * sizeof(double), cudaMemcpyDeviceToHost, g.stream));
   }
@@ -630,12 +654,16 @@ extern "C" int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, doubl
   q.dt = (p->dt > 0) ? p->dt : 1e-4;
   q.diag_every = 0;
   q.tile = -1; q.zdepth = 0;
-  pcgb_box* b = pcgb_box_create(&q);
-  if (!b) return g_err;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0); cudaEventCreate(&e1);
-  double best = 1e30; int bt = b->tile, bz = b->zd;
-  for (int t = 0; t < kNumTiles; ++t) {
+  double best = 1e30; int bt = -1, bz = 0;
+  const int ntile = num_tiles(p->precision);
+  for (int fam = 0; fam < (p->precision == 4 ? 2 : 1); ++fam) {
+  q.tile = fam * kNumScalarTiles;
+  pcgb_box* b = pcgb_box_create(&q);
+  if (!b) { cudaEventDestroy(e0); cudaEventDestroy(e1); return g_err; }
+  if (bt < 0) { bt = b->tile; bz = b->zd; }
+  for (int t = fam * kNumScalarTiles; t < (fam + 1) * kNumScalarTiles && t < ntile; ++t) {
     KernelHandle kh = get_kernel(b->tb, b->nf, t);
     if (!kh.fn || kh.smem > g.max_smem) continue;
     std::vector<int> zs = {b->nz, 256, 128, 64, 32, 16};
@@ -657,8 +685,9 @@ extern "C" int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, doubl
       if (per < best) { best = per; bt = t; bz = zd; }
     }
   }
-  cudaEventDestroy(e0); cudaEventDestroy(e1);
   pcgb_box_destroy(b);
+  }
+  cudaEventDestroy(e0); cudaEventDestroy(e1);
   g_tune[key] = std::make_tuple(bt, bz, best);
   if (tile) *tile = bt;
   if (zdepth) *zdepth = bz;

@@ -257,9 +257,9 @@ class Box:
         return int(load().pcgb_box_bytes(self.h))
 
     def info(self) -> dict:
-        v = (C.c_int * 10)()
-        check(load().pcgb_box_info(self.h, v, 10))
-        keys = ["nx", "ny", "nz", "nf", "bytes_per_value", "tile", "zdepth", "tiles", "px", "xoff"]
+        v = (C.c_int * 11)()
+        check(load().pcgb_box_info(self.h, v, 11))
+        keys = ["nx", "ny", "nz", "nf", "bytes_per_value", "tile", "zdepth", "tiles", "px", "xoff", "pairs"]
         return dict(zip(keys, list(v)))
 
 

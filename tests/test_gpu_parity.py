@@ -152,9 +152,11 @@ def test_diagnostics_fp64(pc, ic, orc):
         assert abs(got - ref) <= TOLDIAG * max(abs(ref), 1e-300), (k, got, ref)
 
 
-def test_isothermal_fp32_compensated(pc, ic, orc):
-    """FP32 state with the compensated 2N accumulation, within 1e-5 of the FP64 oracle."""
-    p = iso_params(pc, precision=4, comp=1)
+@pytest.mark.parametrize("tile", [0, 4, 5, 6, 7])
+def test_isothermal_fp32_compensated(pc, ic, orc, tile):
+    """FP32 state with the compensated 2N accumulation, within 1e-5 of the FP64 oracle,
+    in the field-major layout (tile 0) and the packed field-pair layout (tiles 4-7)."""
+    p = iso_params(pc, precision=4, comp=1, tile=tile)
     p.update(nu=5e-3, eta=5e-3)
     f0 = iso_state(pc, ic, p)
     ic.abc_flow(f0, p, ampl=0.1)
@@ -167,9 +169,10 @@ def test_isothermal_fp32_compensated(pc, ic, orc):
     assert np.all(err <= TOL32), err
 
 
-def test_entropy_fp32(pc, ic, orc):
+@pytest.mark.parametrize("tile", [0, 4])
+def test_entropy_fp32(pc, ic, orc, tile):
     p = pc.default_params(nx=32, ny=32, nz=32, lentropy=1, gamma=5.0 / 3.0, nu=2e-3, eta=2e-3, chi=2e-3,
-                          dt=1e-3, precision=4, comp=1)
+                          dt=1e-3, precision=4, comp=1, tile=tile)
     f0 = ic.zeros(p)
     ic.abc_flow(f0, p, ampl=1.0, A=0.1, B=0.1, C=0.1, k=1.0)
     ic.gaussian_noise(f0, p, ["ax", "ay", "az"], 1e-4, 7)
@@ -210,3 +213,23 @@ def test_tiles_cross_agree(pc, ic):
         outs.append(box.store())
     for g in outs[1:]:
         assert np.all(rel_err(g, outs[0]) <= 1e-14)
+
+
+def test_fp32_pair_layout_diagnostics_and_cfl(pc, ic, orc):
+    """Packed-pair FP32 kernel: diagnostics (FP64 sums of FP32 cell values) and the lagged CFL
+    dt agree with the FP64 oracle to FP32 round-off."""
+    p = iso_params(pc, precision=4, comp=1, tile=4, dt=0.0, dt_mode=2, cdt=0.4, diag_every=1,
+                   b_ext=(0.0, 0.1, 0.0), lforcing_cont=1, ampl_ff=0.05, kf=2.0)
+    f0 = iso_state(pc, ic, p, ampl=1e-2, seed=41)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(1)
+    raw = box.diag_raw()
+    t, dt, _ = box.time()
+    op = oracle_params(orc, p)
+    f = np.array(f0, order="F", copy=True)
+    orc.ghosts(op, f)
+    dt1, dg = orc.pde(op, f, np.zeros_like(f), 0.0, want_dt=True, diag=True)
+    assert abs(dt * dt1 - 1.0) <= 1e-6
+    for k in (orc.D_U2SUM, orc.D_B2SUM, orc.D_EKINSUM, orc.D_RHOSUM, orc.D_J2SUM):
+        assert abs(raw[k + 1] - dg[k]) <= 1e-5 * abs(dg[k]), k
