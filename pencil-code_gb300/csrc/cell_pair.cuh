@@ -101,6 +101,7 @@ struct PairCell {
     float fsx, fcx, fsy, fcy;
     const float* sinz;
     const float* cosz;
+    float fsz, fcz;   // sin/cos(kf z) of the current plane, prefetched one plane ahead
     float2 dfnext[4];
 
     __device__ __forceinline__ void begin(const PcgbBoxDev& B, int inb, int x, int y, int z0, bool active,
@@ -117,8 +118,11 @@ struct PairCell {
       const float* cosy = siny + B.my;
       sinz = cosy + B.my;
       cosz = sinz + B.mz;
-      fsx = fcx = fsy = fcy = 0.f;
-      if (forcing && active) { fsx = sinx[x + 3]; fcx = cosx[x + 3]; fsy = siny[y + 3]; fcy = cosy[y + 3]; }
+      fsx = fcx = fsy = fcy = fsz = fcz = 0.f;
+      if (forcing && active) {
+        fsx = sinx[x + 3]; fcx = cosx[x + 3]; fsy = siny[y + 3]; fcy = cosy[y + 3];
+        fsz = sinz[z0 + 3]; fcz = cosz[z0 + 3];
+      }
 #pragma unroll
       for (int p = 0; p < 4; ++p) dfnext[p] = make_float2(0.f, 0.f);
       if (fl.read_df && active && !mode_cfl) {
@@ -192,9 +196,10 @@ struct PairCell {
       }
       float fc[3] = {0.f, 0.f, 0.f};
       if (forcing) {   // forcing_cont 'ABC', forcing.f90:5894-5896
-        fc[0] = P.fact * (P.abc_c * sinz[z + 3] + (P.fact2 * P.abc_b) * fcy);
-        fc[1] = P.fact * (P.abc_a * fsx + (P.fact2 * P.abc_c) * cosz[z + 3]);
+        fc[0] = P.fact * (P.abc_c * fsz + (P.fact2 * P.abc_b) * fcy);
+        fc[1] = P.fact * (P.abc_a * fsx + (P.fact2 * P.abc_c) * fcz);
         fc[2] = P.fact * (P.abc_b * fsy + (P.fact2 * P.abc_a) * fcx);
+        if (z + 1 < z1) { fsz = sinz[z + 4]; fcz = cosz[z + 4]; }
       }
       float dfo[NF], dfn[NF];
       dfo[0] = dfo2[0].x; dfo[1] = dfo2[1].x; dfo[2] = dfo2[2].x; dfo[ILNRHO] = dfo2[3].x;

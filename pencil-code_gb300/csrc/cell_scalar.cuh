@@ -73,6 +73,7 @@ struct ScalarCell {
     T fsx, fcx, fsy, fcy;
     const T* sinz;
     const T* cosz;
+    T fsz, fcz;   // sin/cos(kf z) of the current plane, prefetched one plane ahead
     T dfnext[NF];
 
     __device__ __forceinline__ void begin(const PcgbBoxDev& B, int inb, int x, int y, int z0, bool active,
@@ -89,8 +90,11 @@ struct ScalarCell {
       const T* cosy = siny + B.my;
       sinz = cosy + B.my;
       cosz = sinz + B.mz;
-      fsx = fcx = fsy = fcy = T(0);
-      if (forcing && active) { fsx = sinx[x + 3]; fcx = cosx[x + 3]; fsy = siny[y + 3]; fcy = cosy[y + 3]; }
+      fsx = fcx = fsy = fcy = fsz = fcz = T(0);
+      if (forcing && active) {
+        fsx = sinx[x + 3]; fcx = cosx[x + 3]; fsy = siny[y + 3]; fcy = cosy[y + 3];
+        fsz = sinz[z0 + 3]; fcz = cosz[z0 + 3];
+      }
 #pragma unroll
       for (int k = 0; k < NF; ++k) dfnext[k] = T(0);
       if (fl.read_df && active && !mode_cfl) {
@@ -158,9 +162,10 @@ struct ScalarCell {
       }
       T fc[3] = {T(0), T(0), T(0)};
       if (forcing) {   // forcing_cont 'ABC', forcing.f90:5894-5896
-        fc[0] = P.fact * (P.abc_c * sinz[z + 3] + (P.fact2 * P.abc_b) * fcy);
-        fc[1] = P.fact * (P.abc_a * fsx + (P.fact2 * P.abc_c) * cosz[z + 3]);
+        fc[0] = P.fact * (P.abc_c * fsz + (P.fact2 * P.abc_b) * fcy);
+        fc[1] = P.fact * (P.abc_a * fsx + (P.fact2 * P.abc_c) * fcz);
         fc[2] = P.fact * (P.abc_b * fsy + (P.fact2 * P.abc_a) * fcx);
+        if (z + 1 < z1) { fsz = sinz[z + 4]; fcz = cosz[z + 4]; }
       }
       T dfn[NF];
       cell_rhs<T, NF>(c, P, F, fc, forcing, iso, vheat, oheat, dfo, fl.alpha, dfn, fl.want_cfl, fl.want_diag, acc,

@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
   }
   __syncthreads();
 
-  unsigned long long gplane = 0;   // planes loaded by this CTA so far (ring phase tracking)
+  unsigned int gplane = 0;   // planes loaded by this CTA in this launch (ring slot and phase tracking)
   int iter = 0;
   int failed = 0;
 
@@ -83,7 +83,10 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
       if (args.boxes[mid].tile0 <= w) lo = mid; else hi = mid - 1;
     }
     const PcgbBoxDev& B = args.boxes[lo];
-    PcgbBoxState* S = B.state;
+    PcgbBoxState* const S = B.state;
+    const int btiles = B.tiles;
+    double* const bpartial = B.partial;
+    const int bdt_mode = B.dt_mode;
 
     const int lt = w - B.tile0;
     const int ntx = B.ntx, nty = B.nty;
@@ -114,16 +117,20 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
     fl.cinv = (fl.comp && s < 2) ? T(1.0 / (dt * rk_beta(s + 1) * rk_alpha(s + 1))) : T(0);
     const bool need_red = fl.want_cfl || fl.want_diag;
 
-    // producer: prologue
+    // plane j of this tile is ring plane gplane + j: slot (sbase + j) % RING and
+    // fill phase ((sbase + j) / RING + pbase) & 1
+    const unsigned int sbase = gplane % RING, pbase = gplane / RING;
+    // producer: prologue (TMA box origin held in a register: stores through the
+    // cell's output pointers would otherwise force a reload from the descriptor)
+    const int tma_x = B.xoff + x0 - 4;
     if (tid == 0) {
       prefetch_tensormap(tmap);
       const int npro = nplanes < RING ? nplanes : RING;
       for (int j = 0; j < npro; ++j) {
-        const unsigned long long G = gplane + (unsigned long long)j;
-        const int slot = (int)(G % RING);
+        const unsigned int slot = (sbase + j) % RING;
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&full[slot], C::PLANE_BYTES);
-        tma_load_4d(smem + slot * C::SLOT_BYTES, tmap, &full[slot], B.xoff + x0 - 4, y0, z0 + j, 0);
+        tma_load_4d(smem + slot * C::SLOT_BYTES, tmap, &full[slot], tma_x, y0, z0 + j, 0);
       }
     }
 
@@ -142,8 +149,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
       const int jw0 = (j == 0) ? 0 : j + 6;
       int lfail = 0;
       for (int jw = jw0; jw <= j + 6; ++jw) {
-        const unsigned long long G = gplane + (unsigned long long)jw;
-        if (!mbar_wait_bounded(&full[G % RING], (uint32_t)((G / RING) & 1ull), args.wait_limit)) lfail = 1;
+        const unsigned int r = sbase + (unsigned int)jw;
+        if (!mbar_wait_bounded(&full[r % RING], ((r / RING) + pbase) & 1u, args.wait_limit)) lfail = 1;
       }
       if (__syncthreads_or(lfail)) {
         failed = 1;
@@ -151,8 +158,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
         if (tid == 0) {
           const int hi2 = (j + RING < nplanes) ? j + RING : nplanes;
           for (int jw = j; jw < hi2; ++jw) {
-            const unsigned long long G = gplane + (unsigned long long)jw;
-            mbar_wait_bounded(&full[G % RING], (uint32_t)((G / RING) & 1ull), args.wait_limit);
+            const unsigned int r = sbase + (unsigned int)jw;
+            mbar_wait_bounded(&full[r % RING], ((r / RING) + pbase) & 1u, args.wait_limit);
           }
         }
         break;
@@ -160,10 +167,12 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
 
       if (active) {
         const Elem* pl[7];
+        const unsigned int s0 = (sbase + (unsigned int)j) % RING;
+        const unsigned char* cbase = smem + ((ty + 3) * C::BW + (tx + 4)) * (int)sizeof(Elem);
 #pragma unroll
         for (int d = 0; d < 7; ++d) {
-          const unsigned long long G = gplane + (unsigned long long)(j + d);
-          pl[d] = reinterpret_cast<const Elem*>(smem + (G % RING) * C::SLOT_BYTES) + (ty + 3) * C::BW + (tx + 4);
+          const unsigned int sd = (s0 + d >= (unsigned int)RING) ? s0 + d - RING : s0 + d;
+          pl[d] = reinterpret_cast<const Elem*>(cbase + sd * C::SLOT_BYTES);
         }
         if (!mode_cfl) cell.step(pl, x, y, z, z1, fl, acc, dt1max);
         else cell.cfl(pl, dt1max);
@@ -171,14 +180,13 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
 
       __syncthreads();   // every thread is done with plane j
       if (tid == 0 && j + RING < nplanes) {
-        const unsigned long long G = gplane + (unsigned long long)(j + RING);
-        const int slot = (int)(G % RING);
+        const unsigned int slot = (sbase + (unsigned int)j) % RING;   // the slot plane j just freed
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&full[slot], C::PLANE_BYTES);
-        tma_load_4d(smem + slot * C::SLOT_BYTES, tmap, &full[slot], B.xoff + x0 - 4, y0, z0 + j + RING, 0);
+        tma_load_4d(smem + slot * C::SLOT_BYTES, tmap, &full[slot], tma_x, y0, z0 + j + RING, 0);
       }
     }
-    gplane += (unsigned long long)nplanes;
+    gplane += (unsigned int)nplanes;
     if (failed) {
       if (tid == 0) atomicOr(&S->err, PCGB_ERR_TIMEOUT);
       break;
@@ -198,7 +206,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
       if (tid < PCGB_NSLOT) {
         double r = red[tid];
         for (int wq = 1; wq < C::NWARP; ++wq) r = red_op(tid, r, red[wq * PCGB_NSLOT + tid]);
-        B.partial[(long long)lt * PCGB_NSLOT + tid] = r;
+        bpartial[(long long)lt * PCGB_NSLOT + tid] = r;
       }
     }
 
@@ -207,7 +215,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
     __syncthreads();
     if (tid == 0) {
       const unsigned int prev = atomicAdd(&S->done, 1u);
-      sh[1] = (prev == (unsigned int)(B.tiles - 1)) ? 1 : 0;
+      sh[1] = (prev == (unsigned int)(btiles - 1)) ? 1 : 0;
     }
     __syncthreads();
     if (sh[1]) {
@@ -216,10 +224,10 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
         double part[PCGB_NSLOT];
 #pragma unroll
         for (int q = 0; q < PCGB_NSLOT; ++q) part[q] = 0.0;
-        for (int t = tid; t < B.tiles; t += C::NT) {
+        for (int t = tid; t < btiles; t += C::NT) {
 #pragma unroll
           for (int q = 0; q < PCGB_NSLOT; ++q)
-            part[q] = red_op(q, part[q], __ldcg(&B.partial[(long long)t * PCGB_NSLOT + q]));
+            part[q] = red_op(q, part[q], __ldcg(&bpartial[(long long)t * PCGB_NSLOT + q]));
         }
 #pragma unroll
         for (int q = 0; q < PCGB_NSLOT; ++q) {
@@ -239,7 +247,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
             const double dtn = 1.0 / r[PCGB_S_DT1MAX];   // set_dt, sub.f90:4247
             if (!(dtn > 0.0) || !isfinite(dtn)) atomicOr(&S->err, PCGB_ERR_DT | PCGB_ERR_NONFINITE);
             if (mode_cfl) {
-              if (B.dt_mode != PCGB_DT_FIXED) { S->dt = dtn; S->dt_next = dtn; }
+              if (bdt_mode != PCGB_DT_FIXED) { S->dt = dtn; S->dt_next = dtn; }
             } else {
               S->dt_next = dtn;
             }
@@ -258,7 +266,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
           ds = ds + 1.0;
           S->ds = ds;
           S->t = S->t + ds * (dt * rk_beta(s));
-          if (s == 2 && B.dt_mode == PCGB_DT_LAGGED) S->dt = S->dt_next;
+          if (s == 2 && bdt_mode == PCGB_DT_LAGGED) S->dt = S->dt_next;
           S->nsub = nsub + 1ull;
         }
         S->done = 0u;
