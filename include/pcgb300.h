@@ -216,6 +216,8 @@ int pcgb_box_time(pcgb_box* b, double* t, double* dt, long long* nsub);
 int pcgb_box_set_dt(pcgb_box* b, double dt);
 /* Device bytes held by the box. */
 size_t pcgb_box_bytes(const pcgb_box* b);
+/* Device bytes a box with these parameters would hold (admission control). */
+size_t pcgb_params_bytes(const pcgb_params* p);
 /* Cells, fields, precision and tile of the box. */
 int pcgb_box_info(const pcgb_box* b, int* info, int ninfo);
 
@@ -226,6 +228,30 @@ void pcgb_batch_destroy(pcgb_batch* b);
 /* nsteps RK3 steps for every box; use_graph != 0 captures the substep loop
    of graph_steps steps in a CUDA graph and replays it. */
 int pcgb_batch_steps(pcgb_batch* b, int nsteps, int use_graph, int graph_steps);
+
+/* Request server with continuous batching.  Requests (a parameter block,
+   a step count and a seeded initial condition) are admitted in arrival order
+   while their device memory fits the budget; admitted boxes advance together,
+   one persistent launch per substep per class (precision, field count), in
+   rounds of at most round_steps RK3 steps; boxes that finish leave and
+   waiting requests join between rounds.  max_active = 1 gives FIFO
+   one-at-a-time service.  Times are seconds since the server was created. */
+typedef struct pcgb_server pcgb_server;
+pcgb_server* pcgb_server_create(size_t mem_budget_bytes, int max_active, int round_steps);
+/* init: Gaussian noise of amplitude noise_ampl on aa (seeded), ABC flow of
+   amplitude abc_ampl on uu when abc_ampl != 0.  f_out, if not NULL, receives
+   the final f(mx,my,mz,nf) (double, Fortran order).  Returns a request id >= 0. */
+long long pcgb_server_submit(pcgb_server* s, const pcgb_params* p, int nsteps, unsigned long long seed,
+                             double noise_ampl, double abc_ampl, double* f_out);
+/* 1 when request id is done (times[0..2] = submitted, started, finished;
+   diag[0..PCGB_NSLOT+2] = the box's last reduced slots, t, dt, step), 0 while
+   pending, < 0 on error. */
+int pcgb_server_poll(pcgb_server* s, long long id, double* times, double* diag);
+/* Wait until every submitted request is done or timeout_s passes (0: done). */
+int pcgb_server_drain(pcgb_server* s, double timeout_s);
+/* stats[0..5] = submitted, completed, active now, peak active, peak device bytes, rounds. */
+int pcgb_server_stats(pcgb_server* s, double* stats, int nstats);
+void pcgb_server_destroy(pcgb_server* s);
 
 /* Autotuner: times each tile variant and z-depth for a box of this shape and
    returns the best (tile, zdepth); results are cached per (precision, nf, n). */

@@ -319,6 +319,22 @@ extern "C" void pcgb_box_destroy(pcgb_box* b) {
   box_free(b);
 }
 
+// Device bytes a box with these parameters will hold (same layout as pcgb_box_create).
+extern "C" size_t pcgb_params_bytes(const pcgb_params* p) {
+  if (!p || p->nx < 1 || p->ny < 1 || p->nz < 1 || (p->precision != 4 && p->precision != 8)) return 0;
+  const int tb = p->precision, nf = p->lentropy ? 8 : 7;
+  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb);
+  const int pairs = (t0 < num_tiles(tb) && tile_is_pair(tb, t0)) ? 1 : 0;
+  const int eb = pairs ? 8 : tb, ns = pairs ? 4 : nf;
+  const int xoff = 128 / eb;
+  const long long px = xoff + ((p->nx + 8 + xoff - 1) / xoff) * xoff;
+  const long long fs = px * (p->ny + 6) * (p->nz + 6);
+  const size_t fbytes = (size_t)fs * ns * eb;
+  const long long ntiles = (long long)((p->nx + 15) / 16) * ((p->ny + 1) / 2) * 64;   // upper bound on tiles
+  return 3 * fbytes + (size_t)ntiles * PCGB_NSLOT * 8 / 64 + 4096 +
+         (2 * (size_t)px + 2 * (size_t)(p->ny + 6) + 2 * (size_t)(p->nz + 6)) * tb;
+}
+
 extern "C" size_t pcgb_box_bytes(const pcgb_box* b) {
   if (!b) return 0;
   return 3 * b->fbytes + (size_t)b->tiles * PCGB_NSLOT * 8 + sizeof(PcgbBoxState) + sizeof(PcgbBoxDev) +

@@ -1,0 +1,67 @@
+"""Continuous-batching server: every request's result is the same served in
+a mix of uneven requests as computed alone (bitwise: a box's arithmetic does
+not depend on what else shares the launch), and admission respects the
+device-memory budget."""
+import importlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _req(pc, n, prec, ent, seed, nu, k):
+    p = pc.default_params(nx=n, ny=n, nz=n, lentropy=int(ent), gamma=5.0 / 3.0 if ent else 1.0, precision=prec,
+                          comp=1, nu=nu, eta=1.3 * nu, chi=nu if ent else 0.0, lforcing_cont=1, ampl_ff=0.03, kf=k,
+                          dt=0.0, dt_mode=1, cdt=0.4)
+    return p
+
+
+def _alone(pc, ens, p, steps, seed):
+    q = pc.default_params()
+    q.update(**p.as_dict())
+    q.tile = 6 if q.precision == 4 else 1
+    q.zdepth = 16
+    b = pc.Box(q)
+    ens.init_box(b, q, seed)
+    b.steps(steps)
+    return b.store()
+
+
+def test_mix_equals_alone(pc):
+    serve = importlib.import_module("pencil-code_gb300.serve")
+    ens = importlib.import_module("pencil-code_gb300.ensemble")
+    specs = [(32, 4, False, 11, 2e-3, 1.0, 7), (48, 8, False, 12, 5e-3, 2.0, 5), (32, 4, True, 13, 3e-3, 3.0, 9),
+             (64, 4, False, 14, 1e-3, 2.0, 4), (16, 8, True, 15, 8e-3, 1.0, 6), (40, 4, False, 16, 4e-3, 1.0, 8)]
+    srv = serve.Server(budget_bytes=20e9, round_steps=3)
+    outs, ids = [], []
+    for n, prec, ent, seed, nu, k, steps in specs:
+        p = _req(pc, n, prec, ent, seed, nu, k)
+        f = np.zeros(pc.host_shape(p), order="F")
+        outs.append(f)
+        ids.append(srv.submit(p, steps, seed, noise=1e-5, f_out=f))
+    assert srv.drain(600)
+    st = srv.stats()
+    for rid in ids:
+        rc, times, _ = srv.poll(rid)
+        assert rc == 1 and times[0] <= times[1] <= times[2]
+    srv.close()
+    assert st["peak_active"] >= 2
+    for (n, prec, ent, seed, nu, k, steps), f in zip(specs, outs):
+        ref = _alone(pc, ens, _req(pc, n, prec, ent, seed, nu, k), steps, seed)
+        assert np.array_equal(f, ref), (n, prec, ent)
+
+
+def test_admission_budget_and_fifo(pc):
+    serve = importlib.import_module("pencil-code_gb300.serve")
+    L = pc.load()
+    reqs = [_req(pc, 32, 4, False, s, 2e-3, 1.0) for s in range(4)]
+    one = L.pcgb_params_bytes(__import__("ctypes").byref(reqs[0]))
+    for max_active, budget, expect_peak in ((1 << 20, 1.5 * one, 1), (1, 100 * one, 1), (1 << 20, 100 * one, 4)):
+        srv = serve.Server(budget_bytes=budget, max_active=max_active, round_steps=2)
+        ids = [srv.submit(p, 4, 100 + i) for i, p in enumerate(reqs)]
+        assert srv.drain(300)
+        assert all(srv.poll(i)[0] == 1 for i in ids)
+        st = srv.stats()
+        srv.close()
+        assert st["peak_active"] == expect_peak and st["peak_bytes"] <= budget
