@@ -352,6 +352,87 @@ def run_e2e(args, pc, gpu, torch, stream, p, nf):
                     "(REAL=double), wall clock"}
 
 
+def run_ensemble(args):
+    """Ensemble workload: args.boxes boxes of uneven sizes and parameters, args.steps RK3 steps
+    each, batched persistent launches under CUDA-graph replay vs the single-box kernel looping
+    over the boxes.  Both legs advance every box by the same number of steps."""
+    import torch
+    pc = importlib.import_module("pencil-code_gb300")
+    ens = importlib.import_module("pencil-code_gb300.ensemble")
+    L = pc.load()
+    stream = torch.cuda.Stream()
+    L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
+    specs = ens.make_ensemble(args.boxes, seed=args.seed, tile=args.tile if args.tile >= 0 else 6)
+    cells = sum(p.nx * p.ny * p.nz for p, _ in specs)
+    out = {}
+    for leg in ("batched", "plain"):
+        boxes = ens.build_boxes(specs)
+        torch.cuda.synchronize()
+        if leg == "batched":
+            batch = pc.Batch(boxes, persistent=True)
+            batch.steps(args.warmup, use_graph=False)
+        else:
+            for b in boxes:
+                b.steps(args.warmup)
+        torch.cuda.synchronize()
+        n0 = L.pcgb_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        if leg == "batched":
+            batch.steps(args.steps, use_graph=True, graph_steps=args.graph_steps)
+        else:
+            for b in boxes:
+                b.steps(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        for b in boxes:
+            b.sync()
+        out[leg] = {"ms": ms, "solves_per_s": len(boxes) * args.steps / args.solve_steps / (ms / 1e3),
+                    "gcell_per_s": cells * 3 * args.steps / (ms / 1e3) / 1e9,
+                    "launches": int(L.pcgb_launch_count() - n0)}
+        if leg == "batched":
+            batch.close()
+        for b in boxes:
+            b.close()
+        torch.cuda.empty_cache()
+    line = {"metric": "ensemble solves/s", "value": out["batched"]["solves_per_s"], "unit": "solves/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (seeded on device)",
+            "config": {"workload": f"{args.boxes} isothermal MHD boxes, sizes from {{32,48,64,96,128}}^3, "
+                                   f"nu,eta log-uniform [1e-3,1e-2], ABC ampl U[0.01,0.05] k in {{1,2,3}}, "
+                                   f"CFL dt cdt=0.4, FP32 state, FP64 reductions",
+                       "solve": f"{args.solve_steps} RK3 steps", "graph_steps": args.graph_steps},
+            "batched": out["batched"], "plain": out["plain"],
+            "speedup_vs_plain": out["batched"]["solves_per_s"] / out["plain"]["solves_per_s"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serve(args):
+    serve = importlib.import_module("pencil-code_gb300.serve")
+    pc = importlib.import_module("pencil-code_gb300")
+    pc.load()
+    res = []
+    for rate in args.rates:
+        reqs = serve.draw_requests(args.requests, seed=args.seed, steps_scale=args.steps_scale,
+                                   fp64_fraction=args.fp64_fraction)
+        row = {"rate": rate}
+        for mode, maxa in (("batched", 1 << 20), ("fifo", 1)):
+            row[mode] = serve.run_stream(reqs, rate, seed=args.seed, max_active=maxa, budget=args.budget_gb * 1e9,
+                                         round_steps=args.round_steps)
+        res.append(row)
+    line = {"metric": "serving solves/s and latency", "unit": "solves/s, s", "n_gpus": 1,
+            "data": "synthetic Poisson request stream",
+            "config": {"requests": args.requests, "sizes": "{32,64,128,256}^3 weights .4/.3/.2/.1",
+                       "physics": "isothermal or entropy p=0.5", "fp64_fraction": args.fp64_fraction,
+                       "steps": f"U[100,2000] x {args.steps_scale}", "budget_gb": args.budget_gb,
+                       "round_steps": args.round_steps},
+            "results": res}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,11 +448,26 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=96)
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
+    ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "serve"])
+    ap.add_argument("--boxes", type=int, default=192)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--graph-steps", type=int, default=10)
+    ap.add_argument("--solve-steps", type=int, default=500)
+    ap.add_argument("--requests", type=int, default=40)
+    ap.add_argument("--rates", type=float, nargs="+", default=[5.0, 50.0])
+    ap.add_argument("--steps-scale", type=float, default=0.1)
+    ap.add_argument("--fp64-fraction", type=float, default=0.5)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--round-steps", type=int, default=10)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ensemble":
+        return run_ensemble(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

