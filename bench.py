@@ -362,11 +362,14 @@ def run_ensemble(args):
     L = pc.load()
     stream = torch.cuda.Stream()
     L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
-    specs = ens.make_ensemble(args.boxes, seed=args.seed, tile=args.tile if args.tile >= 0 else 6)
+    specs = ens.make_ensemble(args.boxes, seed=args.seed)
     cells = sum(p.nx * p.ny * p.nz for p, _ in specs)
+    # batched leg: tile and z-depth from the batched autotuner; plain leg: single-box defaults
+    t_tile, t_zd, table = ens.autotune_batch(specs)
+    tuned = ens.with_tiling(specs, t_tile, t_zd)
     out = {}
     for leg in ("batched", "plain"):
-        boxes = ens.build_boxes(specs)
+        boxes = ens.build_boxes(tuned if leg == "batched" else specs)
         torch.cuda.synchronize()
         if leg == "batched":
             batch = pc.Batch(boxes, persistent=True)
@@ -402,7 +405,9 @@ def run_ensemble(args):
             "config": {"workload": f"{args.boxes} isothermal MHD boxes, sizes from {{32,48,64,96,128}}^3, "
                                    f"nu,eta log-uniform [1e-3,1e-2], ABC ampl U[0.01,0.05] k in {{1,2,3}}, "
                                    f"CFL dt cdt=0.4, FP32 state, FP64 reductions",
-                       "solve": f"{args.solve_steps} RK3 steps", "graph_steps": args.graph_steps},
+                       "solve": f"{args.solve_steps} RK3 steps", "graph_steps": args.graph_steps,
+                       "autotuned": {"tile": t_tile, "zdepth": t_zd,
+                                     "ms_per_step": {f"{k[0]}/{k[1]}": round(v, 3) for k, v in table.items()}}},
             "batched": out["batched"], "plain": out["plain"],
             "speedup_vs_plain": out["batched"]["solves_per_s"] / out["plain"]["solves_per_s"]}
     print(json.dumps(line), flush=True)

@@ -294,6 +294,13 @@ int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, double* ms_per_s
 int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double dt, const void* f_in, void* f_out, void* df,
                          double* reductions, void* stream);
 
+/* Iteration limit of every bounded wait on a TMA copy inside the substep
+   kernel (0 restores the default, about a second).  When a wait runs out the
+   kernel records PCGB_ERR_TIMEOUT in the box state, waits for its own copies
+   still in flight, and returns; the next pcgb_box_sync/store reports the
+   error and the box must be reloaded.  Used by the failure-detection tests. */
+void pcgb_set_wait_limit(unsigned int iterations);
+
 /* Number of kernel launches issued by this process (all entry points). */
 long long pcgb_launch_count(void);
 /* Name of the compiled device architecture and library version. */

@@ -26,6 +26,10 @@
 
 namespace pcgb {
 
+// Bound of the wait for copies still in flight after a failed wait: long
+// enough for any TMA load to land, so a CTA never leaves with copies pending.
+constexpr unsigned int kDrainWaitLimit = 1u << 26;
+
 template <class CELL, int TX, int TY, int RING>
 struct DriverCfg {
   using Elem = typename CELL::Elem;
@@ -159,7 +163,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
           const int hi2 = (j + RING < nplanes) ? j + RING : nplanes;
           for (int jw = j; jw < hi2; ++jw) {
             const unsigned int r = sbase + (unsigned int)jw;
-            mbar_wait_bounded(&full[r % RING], ((r / RING) + pbase) & 1u, args.wait_limit);
+            mbar_wait_bounded(&full[r % RING], ((r / RING) + pbase) & 1u, kDrainWaitLimit);
           }
         }
         break;

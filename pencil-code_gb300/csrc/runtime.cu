@@ -757,6 +757,9 @@ extern "C" void* pcgb_get_stream(void) {
   return (void*)g.stream;
 }
 extern "C" long long pcgb_launch_count(void) { return g.launches; }
+extern "C" void pcgb_set_wait_limit(unsigned int iterations) {
+  g.wait_limit = iterations ? iterations : (1u << 26);
+}
 extern "C" const char* pcgb_version(void) { return "pcgb300 1.0 sm_103a"; }
 
 // ---------------------------------------------------------------------------

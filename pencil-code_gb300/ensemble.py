@@ -12,12 +12,12 @@ from __future__ import annotations
 
 import numpy as np
 
-from .lib import Batch, Box, default_params
+from .lib import Batch, Box, default_params, load
 
 SIZES = (32, 48, 64, 96, 128)
 
 
-def make_ensemble(nboxes: int = 192, seed: int = 0, precision: int = 4, tile: int = 6, zdepth: int = 16):
+def make_ensemble(nboxes: int = 192, seed: int = 0, precision: int = 4, tile: int = -1, zdepth: int = 0):
     rng = np.random.Generator(np.random.PCG64(seed))
     specs = []
     for i in range(nboxes):
@@ -60,3 +60,58 @@ def run_plain(boxes, steps: int):
     for b in boxes:
         b.steps(steps)
     boxes[0].sync()
+
+
+def autotune_batch(specs, tiles=(4, 5, 6, 7), zdepths=(16, 32, 64), steps: int = 3, sample: int = 24):
+    """Pick the tile variant and z-sweep depth for batched launches of this ensemble by
+    timing a sample of its boxes (every size present) in persistent launches.
+    Returns (tile, zdepth, table of ms per step)."""
+    import torch
+    by_size = {}
+    for p, seed in specs:
+        by_size.setdefault(p.nx, []).append((p, seed))
+    pick = []
+    i = 0
+    while len(pick) < min(sample, len(specs)):
+        for n in sorted(by_size):
+            lst = by_size[n]
+            if i < len(lst) and len(pick) < sample:
+                pick.append(lst[i])
+        i += 1
+    table = {}
+    for tile in tiles:
+        for zd in zdepths:
+            boxes = []
+            for p, seed in pick:
+                q = default_params()
+                q.update(**p.as_dict())
+                q.tile, q.zdepth = tile, zd
+                b = Box(q)
+                init_box(b, q, seed)
+                boxes.append(b)
+            batch = Batch(boxes, persistent=True)
+            batch.steps(1, use_graph=False)
+            torch.cuda.synchronize()
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            stream = torch.cuda.ExternalStream(load().pcgb_get_stream())
+            t0.record(stream)
+            batch.steps(steps, use_graph=False)
+            t1.record(stream)
+            torch.cuda.synchronize()
+            table[(tile, zd)] = t0.elapsed_time(t1) / steps
+            batch.close()
+            for b in boxes:
+                b.close()
+    best = min(table, key=table.get)
+    return best[0], best[1], table
+
+
+def with_tiling(specs, tile: int, zdepth: int):
+    out = []
+    for p, seed in specs:
+        q = default_params()
+        q.update(**p.as_dict())
+        q.tile, q.zdepth = tile, zdepth
+        out.append((q, seed))
+    return out
