@@ -300,6 +300,10 @@ int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double dt, const vo
    still in flight, and returns; the next pcgb_box_sync/store reports the
    error and the box must be reloaded.  Used by the failure-detection tests. */
 void pcgb_set_wait_limit(unsigned int iterations);
+/* Test hook: when on, every plane wait of the substep kernel also waits (with
+   the same bound) on a shared-memory barrier that nothing ever arrives on, so
+   the bounded wait runs out and the timeout path above is taken. */
+void pcgb_inject_wait_failure(int on);
 
 /* Number of kernel launches issued by this process (all entry points). */
 long long pcgb_launch_count(void);

@@ -16,6 +16,7 @@ struct LaunchArgs {
   unsigned int* work_counter; // non-null: persistent CTAs pull tiles from this counter
   int mode;                   // MODE_SUBSTEP or MODE_CFL
   unsigned int wait_limit;    // bounded mbarrier wait (iterations)
+  int inject_wait_failure;    // test hook: also wait on a barrier nothing arrives on
 };
 
 // Williamson (1980) low-storage RK3, timestep.f90:43-44.

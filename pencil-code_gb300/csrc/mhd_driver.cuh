@@ -39,7 +39,7 @@ struct DriverCfg {
   static constexpr int BH = TY + 6;   // TMA box rows:  y0-3 .. y0+TY+3
   static constexpr int PLANE_BYTES = CELL::NSLICE * BW * BH * (int)sizeof(Elem);
   static constexpr int SLOT_BYTES = (PLANE_BYTES + 127) / 128 * 128;
-  static constexpr int RED_OFF = RING * SLOT_BYTES + RING * 8;
+  static constexpr int RED_OFF = RING * SLOT_BYTES + (RING + 1) * 8;   // RING slot barriers + one never armed
   static constexpr int SMEM_BYTES = RED_OFF + NWARP * PCGB_NSLOT * 8 + 64;
 };
 
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
   const int lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0) {
-    for (int r = 0; r < RING; ++r) mbar_init(&full[r], 1);
+    for (int r = 0; r <= RING; ++r) mbar_init(&full[r], 1);   // full[RING]: never arrived on
     fence_mbar_init();
   }
   __syncthreads();
@@ -156,6 +156,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
         const unsigned int r = sbase + (unsigned int)jw;
         if (!mbar_wait_bounded(&full[r % RING], ((r / RING) + pbase) & 1u, args.wait_limit)) lfail = 1;
       }
+      // failure-detection test hook: a flag that nothing sets, waited for with the same bound
+      if (args.inject_wait_failure && !mbar_wait_bounded(&full[RING], 0u, args.wait_limit)) lfail = 1;
       if (__syncthreads_or(lfail)) {
         failed = 1;
         // drain: wait (bounded) for every plane still in flight before leaving

@@ -186,7 +186,7 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
 
   LaunchArgs a;
   a.boxes = d_desc; a.nboxes = 1; a.total_tiles = h.tiles; a.work_counter = nullptr;
-  a.mode = MODE_SUBSTEP; a.wait_limit = 1u << 26;
+  a.mode = MODE_SUBSTEP; a.wait_limit = 1u << 26; a.inject_wait_failure = 0;
   void* args[] = {&a};
   if (cudaLaunchKernel(kh.fn, dim3(h.tiles), dim3(kh.threads), args, (size_t)kh.smem, s) != cudaSuccess)
     return fail(1, "kernel launch failed");

@@ -82,6 +82,7 @@ struct Engine {
   double* stage = nullptr;        // host-layout staging buffer
   size_t stage_elems = 0;
   unsigned int wait_limit = 1u << 26;
+  int inject_wait_failure = 0;
 };
 static Engine g;
 
@@ -360,6 +361,7 @@ static int launch(const PcgbBoxDev* dboxes, int nboxes, int total_tiles, unsigne
   a.work_counter = counter;
   a.mode = mode;
   a.wait_limit = g.wait_limit;
+  a.inject_wait_failure = g.inject_wait_failure;
   if (counter) CK(cudaMemsetAsync(counter, 0, sizeof(unsigned int), g.stream));
   void* args[] = {&a};
   CK(cudaLaunchKernel(kh.fn, dim3(grid), dim3(kh.threads), args, (size_t)kh.smem, g.stream));
@@ -760,6 +762,7 @@ extern "C" long long pcgb_launch_count(void) { return g.launches; }
 extern "C" void pcgb_set_wait_limit(unsigned int iterations) {
   g.wait_limit = iterations ? iterations : (1u << 26);
 }
+extern "C" void pcgb_inject_wait_failure(int on) { g.inject_wait_failure = on ? 1 : 0; }
 extern "C" const char* pcgb_version(void) { return "pcgb300 1.0 sm_103a"; }
 
 // ---------------------------------------------------------------------------

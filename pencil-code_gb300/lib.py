@@ -78,7 +78,7 @@ EXPORTS = [
     "pcgb_box_create", "pcgb_box_destroy", "pcgb_box_load", "pcgb_box_store", "pcgb_box_init_field", "pcgb_box_steps",
     "pcgb_box_sync", "pcgb_box_diag", "pcgb_box_time", "pcgb_box_set_dt", "pcgb_box_bytes",
     "pcgb_box_info", "pcgb_batch_create", "pcgb_batch_destroy", "pcgb_batch_steps", "pcgb_autotune",
-    "pcgb_launch_count", "pcgb_version", "pcgb_substep_noalloc", "pcgb_params_bytes", "pcgb_set_wait_limit",
+    "pcgb_launch_count", "pcgb_version", "pcgb_substep_noalloc", "pcgb_params_bytes", "pcgb_set_wait_limit", "pcgb_inject_wait_failure",
     "pcgb_server_create", "pcgb_server_submit", "pcgb_server_poll", "pcgb_server_drain", "pcgb_server_stats",
     "pcgb_server_destroy",
 ]
@@ -149,6 +149,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "pcgb_substep_noalloc": (C.c_int, [P, C.c_int, C.c_double, vp, vp, vp, dptr, vp]),
         "pcgb_params_bytes": (C.c_size_t, [P]),
         "pcgb_set_wait_limit": (None, [C.c_uint]),
+        "pcgb_inject_wait_failure": (None, [C.c_int]),
         "pcgb_server_create": (vp, [C.c_size_t, C.c_int, C.c_int]),
         "pcgb_server_submit": (C.c_longlong, [vp, P, C.c_int, C.c_ulonglong, C.c_double, C.c_double, vp]),
         "pcgb_server_poll": (C.c_int, [vp, C.c_longlong, dptr, dptr]),

@@ -1,8 +1,9 @@
 """Failure detection on the GPU without faulting it.
 
-* A bounded TMA wait that runs out (its limit set to one iteration) makes the
-  kernel record a timeout in the box state, wait for its own copies, and
-  return; the host reads the status, and the same context keeps working.
+* A bounded wait that runs out (on a barrier nothing arrives on, limit 2000
+  iterations) makes the kernel record a timeout in the box state, wait for
+  its own TMA copies, and return; the host reads the status, and the same
+  context keeps working.
 * A NaN planted in the host f-array before upload gives a non-finite CFL
   timestep, which the kernel flags instead of propagating silently."""
 import numpy as np
@@ -12,7 +13,8 @@ pytestmark = pytest.mark.gpu
 
 
 def _box(pc, ic, **kw):
-    p = pc.default_params(nx=32, ny=32, nz=32, gamma=1.0, nu=5e-3, eta=5e-3, dt=5e-3, precision=8, **kw)
+    p = pc.default_params(nx=32, ny=32, nz=32, gamma=1.0, nu=5e-3, eta=5e-3, dt=5e-3, precision=8)
+    p.update(**kw)
     f = ic.zeros(p)
     ic.gaussian_noise(f, p, ["ux", "uy", "uz", "ax", "ay", "az"], 1e-3, 3)
     b = pc.Box(p)
@@ -24,11 +26,13 @@ def test_bounded_wait_timeout_is_reported_and_recoverable(pc, ic):
     L = pc.load()
     b, f = _box(pc, ic)
     try:
-        L.pcgb_set_wait_limit(1)
+        L.pcgb_set_wait_limit(2000)
+        L.pcgb_inject_wait_failure(1)
         b.steps(1)
         with pytest.raises(pc.PcgbError, match="bounded device wait"):
             b.sync()
     finally:
+        L.pcgb_inject_wait_failure(0)
         L.pcgb_set_wait_limit(0)
         L.pcgb_clear_error()
     # the context is usable: reload and step normally
