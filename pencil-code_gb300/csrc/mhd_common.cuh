@@ -96,7 +96,9 @@ __device__ __forceinline__ double red_op(int q, double a, double b) {
 template <typename T>
 __device__ __forceinline__ T cfl_dt1(const Phys<T>& P, const Fac<T>& F, const T u[3], const T bb[3], T rho1, T cs2) {
   T advec_uu = (tabs(u[0]) * F.dx1 + tabs(u[1]) * F.dy1) + tabs(u[2]) * F.dz1;
-  T maxadvec = advec_uu > T(0) ? advec_uu : T(0);
+  // NaN-propagating max(0, advec_uu): a non-finite state must reach the dt
+  // check (the reference stops on notanumber(p%advec_uu), hydro.f90:3510)
+  T maxadvec = (advec_uu > T(0) || advec_uu != advec_uu) ? advec_uu : T(0);
   T t0 = bb[0] * F.dx1, t1 = bb[1] * F.dy1, t2 = bb[2] * F.dz1;
   T advec_va2 = (((t0 * t0 + t1 * t1) + t2 * t2) * P.mu01) * rho1;
   T advec_cs2 = cs2 * F.dxyz2;

@@ -12,7 +12,14 @@ nowhere else):
 2. mhd_abcforcing_ref.json -- the it / dt / urms / umax / brms columns of
    samples/MHD-ABCforcing/reference.out, the reference's regression series
    for isothermal MHD with continuous ABC forcing, with the run parameters of
-   that sample's start.in / run.in.
+   that sample's start.in / run.in, and the text of those two namelist files.
+3. var_sample_1d.dat / var_sample_1d.json -- the var.dat snapshot committed
+   with samples/1d-tests/axionSU2back_lhubble2 (data/proc0), copied as bytes,
+   and what the reference's own Fortran record reader
+   (python/pencil/read/fortran_file.py, FortranFileExt) reads from it.
+4. var_subrecords.json -- a small snapshot written by
+   pencil-code_gb300/vardat.py with a tiny subrecord size, checked at
+   generation time to read back identically through FortranFileExt.
 """
 import importlib.util
 import json
@@ -27,6 +34,14 @@ sys.dont_write_bytecode = True   # never write __pycache__ into the read-only tr
 def load_der_module(ref_root):
     path = os.path.join(ref_root, "python", "pencil", "math", "derivatives", "der_6th_order_w_ghosts.py")
     spec = importlib.util.spec_from_file_location("ref_der6", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def load_fortran_file_module(ref_root):
+    path = os.path.join(ref_root, "python", "pencil", "read", "fortran_file.py")
+    spec = importlib.util.spec_from_file_location("ref_fortran_file", path)
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
     return mod
@@ -78,8 +93,58 @@ def main(ref_root):
               "iforcing_cont": "ABC", "b_ext": [0.0, 0.1, 0.0], "cdt": 0.4, "amplaa": 1e-2,
               "initaa": "gaussian-noise", "nt": 51, "it1": 10,
               "source": "samples/MHD-ABCforcing/{start.in,run.in,print.in,reference.out}"}
+    namelists = {}
+    for name in ("start.in", "run.in"):
+        with open(os.path.join(sample, name)) as fh:
+            namelists[name] = fh.read()
     with open(os.path.join(here, "mhd_abcforcing_ref.json"), "w") as fh:
-        json.dump({"params": params, "series": rows}, fh, indent=1)
+        json.dump({"params": params, "series": rows, "namelists": namelists}, fh, indent=1)
+
+    # var.dat of a sample run, read by the reference's record reader
+    ff = load_fortran_file_module(ref_root)
+    sdir = os.path.join(ref_root, "samples", "1d-tests", "axionSU2back_lhubble2", "data")
+    with open(os.path.join(sdir, "dim.dat")) as fh:
+        mx, my, mz, mvar = (int(v) for v in fh.readline().split()[:4])
+    src = os.path.join(sdir, "proc0", "var.dat")
+    with open(src, "rb") as fh:
+        raw = fh.read()
+    with open(os.path.join(here, "var_sample_1d.dat"), "wb") as fh:
+        fh.write(raw)
+    fr = ff.FortranFileExt(src, header_dtype=np.int32)   # as varfile.py:838 opens it
+    f = fr.read_record("<f8").reshape((mx, my, mz, mvar), order="F")
+    g = fr.read_record("<f8")
+    fr.close()
+    summary = {"dim": [mx, my, mz, mvar], "precision": 8, "t": float(g[0]),
+               "x": g[1:1 + mx].tolist(), "y": g[1 + mx:1 + mx + my].tolist(),
+               "z": g[1 + mx + my:1 + mx + my + mz].tolist(),
+               "dxyz": g[1 + mx + my + mz:4 + mx + my + mz].tolist(),
+               "var_sums": f.sum(axis=(0, 1, 2)).tolist(), "var_absmax": np.abs(f).max(axis=(0, 1, 2)).tolist(),
+               "f_row": f[:, 1, 1, 0].tolist(),
+               "source": "samples/1d-tests/axionSU2back_lhubble2/data/{dim.dat,proc0/var.dat}"}
+    with open(os.path.join(here, "var_sample_1d.json"), "w") as fh:
+        json.dump(summary, fh, indent=1)
+
+    # a snapshot written with forced subrecords, read back by the reference's reader
+    sys.path.insert(0, os.path.dirname(os.path.dirname(here)))
+    import importlib
+    vd = importlib.import_module("pencil-code_gb300.vardat")
+    mx, my, mz, nv = 9, 8, 7, 3
+    rng = np.random.Generator(np.random.PCG64(7))
+    f = rng.standard_normal((mx, my, mz, nv))
+    x, y, z = np.arange(mx) * 0.5, np.arange(my) * 0.25, np.arange(mz) * 0.125
+    tmp = os.path.join(here, "_subrec_tmp.dat")
+    vd.write_var(tmp, f, 1.25, x, y, z, 0.5, 0.25, 0.125, max_subrecord=1000)
+    fr = ff.FortranFileExt(tmp, header_dtype=np.int32)
+    f2 = fr.read_record("<f8").reshape((mx, my, mz, nv), order="F")
+    g2 = fr.read_record("<f8")
+    fr.close()
+    with open(tmp, "rb") as fh:
+        size = len(fh.read())
+    os.remove(tmp)
+    assert np.array_equal(f2, f) and g2[0] == 1.25
+    with open(os.path.join(here, "var_subrecords.json"), "w") as fh:
+        json.dump({"dim": [mx, my, mz, nv], "seed": 7, "max_subrecord": 1000, "file_bytes": size,
+                   "ref_reader_sum": float(f2.sum()), "ref_reader_t": float(g2[0])}, fh, indent=1)
 
 
 if __name__ == "__main__":
