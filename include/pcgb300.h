@@ -175,6 +175,15 @@ void radtransfer_gpu_c_(void);
 void get_gpu_reduced_vars_c_(REAL_PCGB* dst);
 void test_bcs_c_(void);
 void split_update_gpu_c_(void);
+/* gpu_astaroth_ansi.c:72-108 -- TorchFort wrappers (no-ops, present for linking). */
+void tf_train_c_(const char* model_name, REAL_PCGB* loss, int* itsub, double* t);
+void tf_infer_c_(const char* model_name, int* itsub);
+void tf_create_model_c_(const char* model_name, const char* config_file_path, int* comm, int* lmpicomm);
+void print_snapshot_c_(void);
+void tf_load_model_c_(const char* model_name, const char* fname);
+void tf_load_model_checkpoint_c_(const char* model_name, const char* checkpoint_dir);
+void tf_save_model_c_(const char* model_name, const char* fname);
+void tf_save_checkpoint_c_(const char* model_name, const char* checkpoint_dir);
 
 /* Timestep of the plug-in's box: the value Fortran's set_dt would receive
    (gpu_astaroth.cc:1618-1634 calls set_dt from C++; a C caller reads it). */

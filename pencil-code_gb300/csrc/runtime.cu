@@ -1040,3 +1040,15 @@ extern "C" void radtransfer_gpu_c_(void) { radTransfer(); }
 extern "C" void get_gpu_reduced_vars_c_(REAL_PCGB* dst) { getGPUReducedVars(dst); }
 extern "C" void test_bcs_c_(void) { testBCs(); }
 extern "C" void split_update_gpu_c_(void) { splitUpdate(1e-15, 1000000); }
+// TorchFort wrappers (gpu_astaroth_ansi.c:72-108): gpu_astaroth.f90 names them as
+// externals, so a link in place of the reference's plug-in needs them; no-ops here.
+extern "C" void tf_train_c_(const char* m, REAL_PCGB* loss, int* itsub, double* t) { tf_train_c_api(m, loss, *itsub, *t); }
+extern "C" void tf_infer_c_(const char* m, int* itsub) { tf_infer_c_api(m, *itsub); }
+extern "C" void tf_create_model_c_(const char* m, const char* cfg, int* comm, int* lmpicomm) {
+  tf_create_model_c_api(m, cfg, *comm, *lmpicomm == 1);
+}
+extern "C" void print_snapshot_c_(void) { print_debug(); }
+extern "C" void tf_load_model_c_(const char* m, const char* f) { tf_load_model_c_api(m, f); }
+extern "C" void tf_load_model_checkpoint_c_(const char* m, const char* d) { tf_load_model_checkpoint_c_api(m, d); }
+extern "C" void tf_save_model_c_(const char* m, const char* f) { tf_save_model_c_api(m, f); }
+extern "C" void tf_save_checkpoint_c_(const char* m, const char* d) { tf_save_checkpoint_c_api(m, d); }

@@ -74,6 +74,8 @@ EXPORTS = [
     "update_on_gpu_vec_by_ind_c_", "update_on_gpu_arr_by_ind_c_", "update_on_gpu_scal_by_name_c_",
     "update_on_gpu_vec_by_name_c_", "update_on_gpu_arr_by_name_c_", "gpu_prepare_for_first_substep_c_",
     "radtransfer_gpu_c_", "get_gpu_reduced_vars_c_", "test_bcs_c_", "split_update_gpu_c_",
+    "tf_train_c_", "tf_infer_c_", "tf_create_model_c_", "print_snapshot_c_", "tf_load_model_c_",
+    "tf_load_model_checkpoint_c_", "tf_save_model_c_", "tf_save_checkpoint_c_",
     "pcgb_get_dt", "pcgb_get_time", "pcgb_request_diagnostics", "pcgb_time_step",
     "pcgb_box_create", "pcgb_box_destroy", "pcgb_box_load", "pcgb_box_store", "pcgb_box_init_field", "pcgb_box_steps",
     "pcgb_box_sync", "pcgb_box_diag", "pcgb_box_time", "pcgb_box_set_dt", "pcgb_box_bytes",

@@ -101,3 +101,31 @@ def test_parameter_validation(pc):
     for bad in (dict(nx=2), dict(precision=2), dict(cdt=0.0), dict(cs0=-1.0), dict(dt=-1.0)):
         p = pc.default_params(**bad)
         assert L.pcgb_set_params(C.byref(p)) != 0, bad
+
+
+# Externals the reference's Fortran GPU module names (src/gpu_astaroth.f90:21-53),
+# gfortran-mangled.  pos_real_ptr_c comes from src/syscalls_ansi.c:422, part of
+# the reference's own syscalls object, not of the plug-in, and is left out.
+FORTRAN_EXTERNALS = [
+    "initialize_gpu_c", "register_gpu_c", "finalize_gpu_c", "get_farray_ptr_gpu_c", "rhs_gpu_c",
+    "before_boundary_gpu_c", "update_after_substep_gpu_c", "radtransfer_gpu_c", "load_farray_c",
+    "reload_gpu_config_c", "copy_farray_c", "update_on_gpu_arr_by_ind_c", "update_on_gpu_scal_by_ind_c",
+    "update_on_gpu_vec_by_ind_c", "gpu_prepare_for_first_substep_c", "get_gpu_reduced_vars_c", "test_bcs_c",
+    "split_update_gpu_c", "tf_train_c", "tf_infer_c", "tf_create_model_c", "print_snapshot_c",
+    "tf_load_model_c", "tf_load_model_checkpoint_c", "tf_save_model_c", "tf_save_checkpoint_c",
+    "update_on_gpu_arr_by_name_c", "update_on_gpu_scal_by_name_c", "update_on_gpu_vec_by_name_c",
+]
+
+
+def test_fortran_module_externals_link(pc):
+    """A program naming every external of the Fortran GPU module links against the library alone."""
+    lib_path = pc.load()._name
+    decls = "\n".join(f"extern void {n}_(void);" for n in FORTRAN_EXTERNALS)
+    refs = ", ".join(f"(void*){n}_" for n in FORTRAN_EXTERNALS)
+    prog = f"{decls}\nvoid* table[] = {{{refs}}};\nint main(void) {{ return table[0] == 0; }}\n"
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "f.c")
+        open(c, "w").write(prog)
+        r = subprocess.run(["gcc", "-o", os.path.join(d, "f"), c, lib_path, "-Wl,--no-undefined"],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
