@@ -13,6 +13,10 @@
 // z-planes.  Every field slice of one ghosted plane (TX+8) x (TY+6) is staged
 // into a ring of RING shared-memory slots by one 4-D TMA load per plane,
 // tracked by one mbarrier per slot; output plane z reads planes z-3..z+3.
+// Warps are not held in lock step: each warp counts itself off a ring plane
+// when it no longer needs it, and the last warp to do so refills the slot
+// with the plane RING ahead, so a warp only waits for data, never for the
+// other warps of its CTA (there is one CTA barrier per tile, not per plane).
 // Work items come from blockIdx (one tile per CTA) or, for persistent batched
 // launches, from an atomic tile counter.
 //
@@ -39,7 +43,9 @@ struct DriverCfg {
   static constexpr int BH = TY + 6;   // TMA box rows:  y0-3 .. y0+TY+3
   static constexpr int PLANE_BYTES = CELL::NSLICE * BW * BH * (int)sizeof(Elem);
   static constexpr int SLOT_BYTES = (PLANE_BYTES + 127) / 128 * 128;
-  static constexpr int RED_OFF = RING * SLOT_BYTES + (RING + 1) * 8;   // RING slot barriers + one never armed
+  static constexpr int BAR_OFF = RING * SLOT_BYTES;                  // RING slot barriers + one never armed
+  static constexpr int CNT_OFF = BAR_OFF + (RING + 1) * 8;           // RING release counters, abort flag, issued
+  static constexpr int RED_OFF = CNT_OFF + ((RING + 2) * 4 + 7) / 8 * 8;
   static constexpr int SMEM_BYTES = RED_OFF + NWARP * PCGB_NSLOT * 8 + 64;
 };
 
@@ -49,7 +55,10 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
   using T = typename CELL::T;
   using Elem = typename CELL::Elem;
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + RING * C::SLOT_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::BAR_OFF);
+  unsigned int* released = reinterpret_cast<unsigned int*>(smem + C::CNT_OFF);   // [RING]
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::CNT_OFF + RING * 4);
+  unsigned int* issued = reinterpret_cast<unsigned int*>(smem + C::CNT_OFF + (RING + 1) * 4);
   double* red = reinterpret_cast<double*>(smem + C::RED_OFF);
   int* sh = reinterpret_cast<int*>(smem + C::RED_OFF + C::NWARP * PCGB_NSLOT * 8);
 
@@ -59,6 +68,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
 
   if (tid == 0) {
     for (int r = 0; r <= RING; ++r) mbar_init(&full[r], 1);   // full[RING]: never arrived on
+    for (int r = 0; r < RING; ++r) released[r] = 0u;
+    *abort_flag = 0;
     fence_mbar_init();
   }
   __syncthreads();
@@ -130,6 +141,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
     if (tid == 0) {
       prefetch_tensormap(tmap);
       const int npro = nplanes < RING ? nplanes : RING;
+      *issued = (unsigned int)npro;
       for (int j = 0; j < npro; ++j) {
         const unsigned int slot = (sbase + j) % RING;
         fence_proxy_async_smem();
@@ -158,16 +170,10 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
       }
       // failure-detection test hook: a flag that nothing sets, waited for with the same bound
       if (args.inject_wait_failure && !mbar_wait_bounded(&full[RING], 0u, args.wait_limit)) lfail = 1;
-      if (__syncthreads_or(lfail)) {
+      // a failed wait in one warp stops every warp of the CTA
+      if (__any_sync(0xffffffffu, lfail)) *abort_flag = 1;
+      if (*abort_flag) {
         failed = 1;
-        // drain: wait (bounded) for every plane still in flight before leaving
-        if (tid == 0) {
-          const int hi2 = (j + RING < nplanes) ? j + RING : nplanes;
-          for (int jw = j; jw < hi2; ++jw) {
-            const unsigned int r = sbase + (unsigned int)jw;
-            mbar_wait_bounded(&full[r % RING], ((r / RING) + pbase) & 1u, kDrainWaitLimit);
-          }
-        }
         break;
       }
 
@@ -184,12 +190,31 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
         else cell.cfl(pl, dt1max);
       }
 
-      __syncthreads();   // every thread is done with plane j
-      if (tid == 0 && j + RING < nplanes) {
-        const unsigned int slot = (sbase + (unsigned int)j) % RING;   // the slot plane j just freed
-        fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&full[slot], C::PLANE_BYTES);
-        tma_load_4d(smem + slot * C::SLOT_BYTES, tmap, &full[slot], tma_x, y0, z0 + j + RING, 0);
+      // this warp is done with ring plane j; the last warp to say so refills its slot
+      __syncwarp();
+      if (lane == 0) {
+        const unsigned int slot = (sbase + (unsigned int)j) % RING;
+        __threadfence_block();
+        const unsigned int prev = atomicAdd(&released[slot], 1u);
+        if (prev == (unsigned int)(C::NWARP - 1)) {
+          __threadfence_block();
+          released[slot] = 0u;
+          if (j + RING < nplanes) {
+            *issued = (unsigned int)(j + RING + 1);
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&full[slot], C::PLANE_BYTES);
+            tma_load_4d(smem + slot * C::SLOT_BYTES, tmap, &full[slot], tma_x, y0, z0 + j + RING, 0);
+          }
+        }
+      }
+    }
+    failed = __syncthreads_or(failed);
+    if (failed && tid == 0) {
+      // drain: wait (bounded) for the newest plane of every slot before leaving
+      const int hi2 = (int)*issued;
+      for (int jw = (hi2 > RING ? hi2 - RING : 0); jw < hi2; ++jw) {
+        const unsigned int r = sbase + (unsigned int)jw;
+        mbar_wait_bounded(&full[r % RING], ((r / RING) + pbase) & 1u, kDrainWaitLimit);
       }
     }
     gplane += (unsigned int)nplanes;

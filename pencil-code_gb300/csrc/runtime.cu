@@ -79,8 +79,11 @@ struct Engine {
   bool own_stream = false;
   PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   long long launches = 0;
-  double* stage = nullptr;        // host-layout staging buffer
+  double* stage[2] = {nullptr, nullptr};   // host-layout staging buffers (copies of one overlap kernels on the other)
   size_t stage_elems = 0;
+  cudaStream_t xfer = nullptr;             // copy stream of the staged transfers
+  cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  int host_mode = 0;                       // 0 auto, 1 always staged, 2 direct when possible (PCGB_HOST_TRANSFER)
   unsigned int wait_limit = 1u << 26;
   int inject_wait_failure = 0;
 };
@@ -108,8 +111,17 @@ static int engine_init() {
   CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
   if (!fn || q != cudaDriverEntryPointSuccess) return set_err(PCGB_E_CUDA, "cuTensorMapEncodeTiled unavailable");
   g.encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  g.stage_elems = (size_t)8 << 20;  // 64 MiB of doubles
-  CK(cudaMalloc(&g.stage, g.stage_elems * sizeof(double)));
+  g.stage_elems = (size_t)16 << 20;  // 2 x 128 MiB of doubles
+  for (int i = 0; i < 2; ++i) {
+    CK(cudaMalloc(&g.stage[i], g.stage_elems * sizeof(double)));
+    CK(cudaEventCreateWithFlags(&g.ev_copied[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&g.ev_free[i], cudaEventDisableTiming));
+  }
+  CK(cudaStreamCreateWithFlags(&g.xfer, cudaStreamNonBlocking));
+  if (const char* e = getenv("PCGB_HOST_TRANSFER")) {
+    if (!strcmp(e, "staged")) g.host_mode = 1;
+    else if (!strcmp(e, "direct")) g.host_mode = 2;
+  }
   g.init = true;
   return 0;
 }
@@ -214,7 +226,8 @@ static int default_zdepth(const pcgb_box* b) {
   return zd;
 }
 
-static int default_tile(int tb) { return tb == 4 ? 4 : 0; }
+// FP32: packed pairs on (16,8) tiles, two CTAs per SM; FP64: (32,4)
+static int default_tile(int tb) { return tb == 4 ? 6 : 0; }
 
 static int set_tiling(pcgb_box* b, int tile, int zd) {
   if (tile < 0) tile = default_tile(b->tb);
@@ -415,17 +428,49 @@ static int box_reset(pcgb_box* b, double t) {
   return 0;
 }
 
+// Device-visible alias of a host f-array, or nullptr when it has to be staged.
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister) is mapped into the
+// device address space: the layout kernels then read or write it directly
+// over the host link, with no staging copy.  Pageable memory is staged.
+static const void* host_alias(const void* h) {
+  if (g.host_mode == 1) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+  return nullptr;
+}
+
 extern "C" int pcgb_box_load(pcgb_box* b, const double* fh, double t) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!b || !fh) return set_err(PCGB_E_ARG, "null argument");
   const long long rows = (long long)b->my * b->mz * b->nf;
-  const long long chunk = (long long)(g.stage_elems / b->mx);
   const int in = cur_in(b);
-  for (long long r0 = 0; r0 < rows; r0 += chunk) {
+  if (const void* dh = host_alias(fh)) {
+    CK(launch_load_rows(b->tb, b->f[in], static_cast<const double*>(dh), 0, rows, b->mx, b->my, b->mz, b->px,
+                        b->xoff, b->nf, b->pairs, g.stream));
+    ++g.launches;
+    return box_reset(b, t);
+  }
+  // staged: copy chunk c into buffer c&1 on the copy stream while the layout
+  // kernel of chunk c-1 runs on the compute stream
+  const long long chunk = (long long)(g.stage_elems / b->mx);
+  CK(cudaEventRecord(g.ev_free[0], g.stream));
+  CK(cudaEventRecord(g.ev_free[1], g.stream));
+  int c = 0;
+  for (long long r0 = 0; r0 < rows; r0 += chunk, ++c) {
+    const int k = c & 1;
     const long long nr = std::min(chunk, rows - r0);
-    CK(cudaMemcpyAsync(g.stage, fh + r0 * b->mx, (size_t)(nr * b->mx) * sizeof(double), cudaMemcpyHostToDevice, g.stream));
-    CK(launch_load_rows(b->tb, b->f[in], g.stage, r0, nr, b->mx, b->my, b->mz, b->px, b->xoff, b->nf, b->pairs,
+    CK(cudaStreamWaitEvent(g.xfer, g.ev_free[k], 0));
+    CK(cudaMemcpyAsync(g.stage[k], fh + r0 * b->mx, (size_t)(nr * b->mx) * sizeof(double), cudaMemcpyHostToDevice,
+                       g.xfer));
+    CK(cudaEventRecord(g.ev_copied[k], g.xfer));
+    CK(cudaStreamWaitEvent(g.stream, g.ev_copied[k], 0));
+    CK(launch_load_rows(b->tb, b->f[in], g.stage[k], r0, nr, b->mx, b->my, b->mz, b->px, b->xoff, b->nf, b->pairs,
                         g.stream));
+    CK(cudaEventRecord(g.ev_free[k], g.stream));
     ++g.launches;
   }
   return box_reset(b, t);
@@ -461,17 +506,35 @@ extern "C" int pcgb_box_store(pcgb_box* b, double* fh) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!b || !fh) return set_err(PCGB_E_ARG, "null argument");
   const long long rows = (long long)b->my * b->mz * b->nf;
-  const long long chunk = (long long)(g.stage_elems / b->mx);
   const int in = cur_in(b);
   // the FP32 carry lives in df between steps (substep counter at a step boundary)
   const void* carry = (b->hdev.comp && (b->nsub % 3) == 0) ? b->df : nullptr;
-  for (long long r0 = 0; r0 < rows; r0 += chunk) {
-    const long long nr = std::min(chunk, rows - r0);
-    CK(launch_store_rows(b->tb, g.stage, b->f[in], carry, r0, nr, b->nx, b->ny, b->nz, b->px, b->my, b->mz, b->xoff,
-                         b->nf, b->pairs, g.stream));
+  if (void* dh = const_cast<void*>(host_alias(fh))) {
+    CK(launch_store_rows(b->tb, static_cast<double*>(dh), b->f[in], carry, 0, rows, b->nx, b->ny, b->nz, b->px,
+                         b->my, b->mz, b->xoff, b->nf, b->pairs, g.stream));
     ++g.launches;
-    CK(cudaMemcpyAsync(fh + r0 * b->mx, g.stage, (size_t)(nr * b->mx) * sizeof(double), cudaMemcpyDeviceToHost, g.stream));
+    CK(cudaStreamSynchronize(g.stream));
+    return box_check_state(b);
   }
+  // staged: the layout kernel of chunk c fills buffer c&1 while chunk c-1 is copied out
+  const long long chunk = (long long)(g.stage_elems / b->mx);
+  CK(cudaEventRecord(g.ev_free[0], g.xfer));
+  CK(cudaEventRecord(g.ev_free[1], g.xfer));
+  int c = 0;
+  for (long long r0 = 0; r0 < rows; r0 += chunk, ++c) {
+    const int k = c & 1;
+    const long long nr = std::min(chunk, rows - r0);
+    CK(cudaStreamWaitEvent(g.stream, g.ev_free[k], 0));
+    CK(launch_store_rows(b->tb, g.stage[k], b->f[in], carry, r0, nr, b->nx, b->ny, b->nz, b->px, b->my, b->mz,
+                         b->xoff, b->nf, b->pairs, g.stream));
+    ++g.launches;
+    CK(cudaEventRecord(g.ev_copied[k], g.stream));
+    CK(cudaStreamWaitEvent(g.xfer, g.ev_copied[k], 0));
+    CK(cudaMemcpyAsync(fh + r0 * b->mx, g.stage[k], (size_t)(nr * b->mx) * sizeof(double), cudaMemcpyDeviceToHost,
+                       g.xfer));
+    CK(cudaEventRecord(g.ev_free[k], g.xfer));
+  }
+  CK(cudaStreamSynchronize(g.xfer));
   CK(cudaStreamSynchronize(g.stream));
   return box_check_state(b);
 }

@@ -76,3 +76,31 @@ def test_plugin_reduced_vars_and_update(pc, ic, orc):
     for k in ("urms", "umax", "brms", "bmax", "ekin", "rhom", "jrms", "abm"):
         assert abs(red[k] - s[k]) <= 1e-12 * abs(s[k]), (k, red[k], s[k])
     assert red["step"] == 0 and abs(red["dt"] - 5e-3) < 1e-18
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tile", [(8, -1), (4, 4), (4, 0)])
+def test_pinned_and_pageable_host_arrays_agree(pc, ic, precision, tile):
+    """Page-locked host arrays are read and written by the layout kernels directly;
+    pageable ones go through the staging buffers.  Both give the same bits."""
+    torch = pytest.importorskip("torch")
+    p = pc.default_params(nx=40, ny=24, nz=16, gamma=1.0, nu=5e-3, eta=5e-3, dt=1e-3, precision=precision, tile=tile,
+                          comp=1 if precision == 4 else 0)
+    f0 = ic.zeros(p)
+    ic.gaussian_noise(f0, p, ["ux", "uy", "uz", "ax", "ay", "az", "lnrho"], 1e-2, 3)
+    shape = pc.host_shape(p)
+    pinned_in = torch.zeros(int(np.prod(shape)), dtype=torch.float64, pin_memory=True)
+    pinned_out = torch.zeros(int(np.prod(shape)), dtype=torch.float64, pin_memory=True)
+    fin = pinned_in.numpy().reshape(shape, order="F")
+    fout = pinned_out.numpy().reshape(shape, order="F")
+    fin[...] = f0
+    a = pc.Box(p)
+    a.load(f0)
+    a.steps(2)
+    ra = a.store()
+    b = pc.Box(p)
+    b.load(fin)
+    b.steps(2)
+    b.store(fout)
+    assert np.array_equal(ra, fout)
+    a.close(); b.close()
