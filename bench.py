@@ -115,8 +115,8 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def headline_params(pc, n: int, precision: int, lentropy: int = 0):
-    p = pc.default_params(nx=n, ny=n, nz=n, lentropy=lentropy, precision=precision, comp=1,
+def headline_params(pc, n: int, precision: int, lentropy: int = 0, dfloat: int = 0):
+    p = pc.default_params(nx=n, ny=n, nz=n, lentropy=lentropy, precision=precision, comp=1, dfloat=dfloat,
                           gamma=1.0 if not lentropy else 5.0 / 3.0, nu=5e-4, eta=5e-4, chi=5e-4 if lentropy else 0.0,
                           dt=2e-4, lforcing_cont=1, ampl_ff=0.02, kf=2.0, relhel=1.0)
     return p
@@ -231,7 +231,7 @@ def run_ours(args):
     L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
 
     n, prec = args.n, args.precision
-    p = headline_params(pc, n, prec, args.lentropy)
+    p = headline_params(pc, n, prec, args.lentropy, args.dfloat)
     if args.tile >= 0:
         p.tile = args.tile
     if args.zdepth > 0:
@@ -289,9 +289,11 @@ def run_ours(args):
             "metric": "Gcell-updates/s per RK substep", "value": value, "unit": "Gcell-updates/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32" if prec == 4 else "f64", "data": "synthetic (seeded on device)",
+            "dtype": "f32" if prec == 4 else ("f32x2 (double-float)" if args.dfloat else "f64"),
+            "data": "synthetic (seeded on device)",
             "config": {"workload": f"{'entropy' if args.lentropy else 'isothermal'} MHD {n}^3, {nf} fields, "
-                                   f"{'FP32 compensated' if prec == 4 else 'FP64'}, nu=eta=5e-4, ABC k=2 ampl 0.02, "
+                                   f"{'FP32 compensated' if prec == 4 else ('FP64-class double-float' if args.dfloat else 'FP64')}"
+                                   f", nu=eta=5e-4, ABC k=2 ampl 0.02, "
                                    f"dt=2e-4", "grid": n, "fields": nf,
                        "tile": info["tile"], "zdepth": info["zdepth"],
                        "l2": "inputs larger than L2 (state %.1f GB)" % (3 * nf * cells * prec / 1e9),
@@ -447,6 +449,8 @@ def main():
     ap.add_argument("--n", type=int, default=1024)
     ap.add_argument("--precision", type=int, default=4, choices=[4, 8])
     ap.add_argument("--lentropy", type=int, default=0)
+    ap.add_argument("--dfloat", type=int, default=0, choices=[0, 1],
+                    help="with --precision 8: double-float state and arithmetic on the FP32 pipes")
     ap.add_argument("--tile", type=int, default=-1)
     ap.add_argument("--zdepth", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")

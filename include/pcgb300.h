@@ -62,6 +62,9 @@ typedef struct pcgb_params {
   int diag_every;          /* device diagnostics every diag_every steps (0: on request only) */
   int tile;                /* kernel tile variant, -1 = choose automatically */
   int zdepth;              /* z-sweep depth, 0 = choose automatically */
+  int dfloat;              /* precision 8 only: 1 = FP64-class state and arithmetic as double-float
+                              pairs (hi + lo FP32, 48-bit significand) on the FP32 pipes instead of
+                              native FP64, whose rate on this GPU is 1/64 of FP32's */
 } pcgb_params;
 
 /* Defaults of the reference (cdata.f90:211,235,239; eos_idealgas.f90:47;

@@ -16,9 +16,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpcgb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels_f32_7.cu", "kernels_f32_8.cu", "kernels_f64_7.cu", "kernels_f64_8.cu",
+SOURCES = ["kernels_f32_7.cu", "kernels_f32_8.cu", "kernels_f64_7.cu", "kernels_f64_8.cu", "kernels_dd_7.cu",
+           "kernels_dd_8.cu",
            "aux_kernels.cu", "runtime.cu", "noalloc.cu", "server.cu"]
-HEADERS = ["mhd_common.cuh", "mhd_driver.cuh", "cell_physics.cuh", "cell_scalar.cuh", "cell_pair.cuh", "kernels.cuh", "pcgb_box.h", "pcgb_ptx.cuh", "aux_kernels.h"]
+HEADERS = ["mhd_common.cuh", "mhd_driver.cuh", "cell_physics.cuh", "cell_scalar.cuh", "cell_pair.cuh", "kernels.cuh", "pcgb_box.h", "pcgb_ptx.cuh", "aux_kernels.h", "dd.cuh"]
 
 
 def nvcc() -> str:
@@ -69,7 +70,7 @@ def _compile(src: str, verbose: bool) -> str:
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(os.cpu_count() or 4, len(srcs)))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
     if (not os.path.exists(LIB) or not _elf_machine_ok(LIB)
             or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs)):

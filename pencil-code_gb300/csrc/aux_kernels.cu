@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "aux_kernels.h"
+#include "dd.cuh"
 
 namespace pcgb {
 
@@ -120,6 +121,8 @@ cudaError_t launch_load_rows(int tbytes, void* f, const double* stage, long long
   const int th = 256, g = grid_for(nr * mx, th);
   if (tbytes == 4)
     load_rows_kernel<float><<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
+  else if (tbytes == kElemDD)
+    load_rows_kernel<dd><<<g, th, 0, s>>>((dd*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
   else
     load_rows_kernel<double><<<g, th, 0, s>>>((double*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
   return cudaGetLastError();
@@ -132,6 +135,9 @@ cudaError_t launch_store_rows(int tbytes, double* stage, const void* f, const vo
   if (tbytes == 4)
     store_rows_kernel<float><<<g, th, 0, s>>>(stage, (const float*)f, (const float*)carry, r0, nr, nx, ny, nz, px, my,
                                               mz, xoff, nf, pairs);
+  else if (tbytes == kElemDD)
+    store_rows_kernel<dd><<<g, th, 0, s>>>(stage, (const dd*)f, nullptr, r0, nr, nx, ny, nz, px, my, mz, xoff, nf,
+                                           pairs);
   else
     store_rows_kernel<double><<<g, th, 0, s>>>(stage, (const double*)f, (const double*)carry, r0, nr, nx, ny, nz, px,
                                                my, mz, xoff, nf, pairs);
@@ -194,6 +200,9 @@ cudaError_t launch_init_field(int tbytes, void* f, int kind, int comp, double am
   if (tbytes == 4)
     init_field_kernel<float><<<g, th, 0, s>>>((float*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my, xoff,
                                               x0, y0, z0, dx, dy, dz, estride);
+  else if (tbytes == kElemDD)
+    init_field_kernel<dd><<<g, th, 0, s>>>((dd*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my, xoff, x0,
+                                           y0, z0, dx, dy, dz, estride);
   else
     init_field_kernel<double><<<g, th, 0, s>>>((double*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my,
                                                xoff, x0, y0, z0, dx, dy, dz, estride);

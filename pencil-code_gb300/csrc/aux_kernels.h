@@ -3,6 +3,9 @@
 #include <cuda_runtime.h>
 
 namespace pcgb {
+// Element codes passed as `tbytes`: 4 float, 8 double, kElemDD double-float
+// (an 8-byte hi/lo pair of floats, dd.cuh).
+constexpr int kElemDD = 16;
 cudaError_t launch_ghost_fill(int tbytes, void* f, int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf,
                               cudaStream_t s);
 // pairs = 1: packed field-pair layout (P0=(ux,ax) P1=(uy,ay) P2=(uz,az) P3=(lnrho,ss)), px/xoff in pair units

@@ -104,7 +104,7 @@ __device__ __forceinline__ void cell_rhs(const CellIn<T>& c, const Phys<T>& P, c
   for (int jj = 0; jj < 3; ++jj) dfu[jj] = alpha * dfo[IUX + jj] - ugu[jj];
 #pragma unroll
   for (int jj = 0; jj < 3; ++jj)
-    dfu[jj] = dfu[jj] + P.nu * ((c.del2u[jj] + T(2) * sglnrho[jj]) + T(1.0 / 3.0) * c.graddivu[jj]);
+    dfu[jj] = dfu[jj] + P.nu * ((c.del2u[jj] + wmul<T>(2, sglnrho[jj])) + T(1.0 / 3.0) * c.graddivu[jj]);
   if (forcing) {
 #pragma unroll
     for (int jj = 0; jj < 3; ++jj) dfu[jj] = dfu[jj] + P.ampl_fc * fc[jj];
@@ -124,10 +124,10 @@ __device__ __forceinline__ void cell_rhs(const CellIn<T>& c, const Phys<T>& P, c
     if (vheat) {                                                                           // viscosity.f90:2765
       T sij2 = sij[0][0] * sij[0][0];                                                      // multm2_sym_mn
       sij2 = sij2 + sij[1][1] * sij[1][1];
-      sij2 = sij2 + T(2) * (sij[1][0] * sij[1][0]);
+      sij2 = sij2 + wmul<T>(2, sij[1][0] * sij[1][0]);
       sij2 = sij2 + sij[2][2] * sij[2][2];
-      sij2 = sij2 + T(2) * (sij[2][0] * sij[2][0]);
-      sij2 = sij2 + T(2) * (sij[2][1] * sij[2][1]);
+      sij2 = sij2 + wmul<T>(2, sij[2][0] * sij[2][0]);
+      sij2 = sij2 + wmul<T>(2, sij[2][1] * sij[2][1]);
       dfs = dfs + TT1 * (P.two_nu * sij2);
     }
     const T gs0 = c.glnrho[0] + glnTT[0], gs1 = c.glnrho[1] + glnTT[1], gs2 = c.glnrho[2] + glnTT[2];

@@ -24,12 +24,12 @@ struct ScalarCell {
     // der_main, deriv.f90:127-129 (x), :140-142 (y), :158-160 (z)
     __device__ __forceinline__ T der(int k, int j) const {
       if (j == 0)
-        return F.fx * ((T(45) * (v(0, k, 0, 1) - v(0, k, 0, -1)) - T(9) * (v(0, k, 0, 2) - v(0, k, 0, -2))) +
+        return F.fx * ((wmul<T>(45, v(0, k, 0, 1) - v(0, k, 0, -1)) - wmul<T>(9, v(0, k, 0, 2) - v(0, k, 0, -2))) +
                        (v(0, k, 0, 3) - v(0, k, 0, -3)));
       if (j == 1)
-        return F.fy * ((T(45) * (v(0, k, 1, 0) - v(0, k, -1, 0)) - T(9) * (v(0, k, 2, 0) - v(0, k, -2, 0))) +
+        return F.fy * ((wmul<T>(45, v(0, k, 1, 0) - v(0, k, -1, 0)) - wmul<T>(9, v(0, k, 2, 0) - v(0, k, -2, 0))) +
                        (v(0, k, 3, 0) - v(0, k, -3, 0)));
-      return F.fz * ((T(45) * (v(1, k, 0, 0) - v(-1, k, 0, 0)) - T(9) * (v(2, k, 0, 0) - v(-2, k, 0, 0))) +
+      return F.fz * ((wmul<T>(45, v(1, k, 0, 0) - v(-1, k, 0, 0)) - wmul<T>(9, v(2, k, 0, 0) - v(-2, k, 0, 0))) +
                      (v(3, k, 0, 0) - v(-3, k, 0, 0)));
     }
     // der2_main 'standard', deriv.f90:39-41, :502-506
@@ -58,7 +58,7 @@ struct ScalarCell {
           t[d - 1] = ((v(d, k, 0, d) - v(d, k, 0, -d)) + v(-d, k, 0, -d)) - v(-d, k, 0, d);
       }
       const T fac = (a == 0 && b == 1) ? F.mxy : ((a == 1 && b == 2) ? F.myz : F.mxz);
-      return fac * ((T(270) * t[0] - T(27) * t[1]) + T(2) * t[2]);
+      return fac * ((wmul<T>(270, t[0]) - wmul<T>(27, t[1])) + wmul<T>(2, t[2]));
     }
   };
 

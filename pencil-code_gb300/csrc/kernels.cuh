@@ -10,7 +10,7 @@ namespace pcgb {
 // Tile variants.  Ids 0..3 use the field-major layout (one value per field per
 // cell); for FP32, ids 4..7 use the packed field-pair layout (cell_pair.cuh).
 //   FP32: 0 (32,4)x2  1 (32,8)  2 (16,8)x2  3 (64,4)  4 pair(32,4)x2  5 pair(32,8)  6 pair(16,8)x2  7 pair(64,4)
-//   FP64: 0 (32,4)  1 (16,8)  2 (16,4)  3 (32,2)
+//   FP64 and double-float: 0 (32,4)  1 (16,8)  2 (16,4)  3 (32,2)
 // "x2" variants ask for two resident CTAs per SM.
 struct TileShape { int tx, ty; };
 constexpr int kNumScalarTiles = 4;
@@ -34,9 +34,13 @@ KernelHandle kernel_f32_7(int tile);
 KernelHandle kernel_f32_8(int tile);
 KernelHandle kernel_f64_7(int tile);
 KernelHandle kernel_f64_8(int tile);
+KernelHandle kernel_dd_7(int tile);
+KernelHandle kernel_dd_8(int tile);
 
-inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile) {
+// dfl: FP64-class state held as double-float pairs (8-byte elements, same tiles as FP64)
+inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile, int dfl = 0) {
   if (dtype_bytes == 4) return nf == 8 ? kernel_f32_8(tile) : kernel_f32_7(tile);
+  if (dfl) return nf == 8 ? kernel_dd_8(tile) : kernel_dd_7(tile);
   return nf == 8 ? kernel_f64_8(tile) : kernel_f64_7(tile);
 }
 

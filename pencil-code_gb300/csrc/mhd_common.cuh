@@ -4,6 +4,7 @@
 #include <math.h>
 #include "pcgb_box.h"
 #include "pcgb_ptx.cuh"
+#include "dd.cuh"
 
 namespace pcgb {
 

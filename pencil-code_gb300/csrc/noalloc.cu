@@ -65,6 +65,7 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
   if (!p || !f_in || !f_out || !df || isubstep < 1 || isubstep > 3 || !(dt > 0.0))
     return fail(2, "invalid argument");
   if (p->precision != 4 && p->precision != 8) return fail(2, "precision must be 4 or 8");
+  if (p->dfloat) return fail(2, "double-float state is not available here (use the box API)");
   if (p->nx < 3 || p->ny < 3 || p->nz < 3 || p->nx > kMaxExtent || p->ny > kMaxExtent || p->nz > kMaxExtent)
     return fail(7, "grid extent outside [3, PCGB_NOALLOC_MAX_EXTENT]");
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -132,6 +132,7 @@ struct pcgb_box {
   pcgb_params p;
   int nf = 7, tb = 8, tile = 0, zd = 0, tx = 32, ty = 4;
   int pairs = 0;   // packed field-pair layout (FP32 tiles 4..7)
+  int dfl = 0;     // FP64-class state as double-float pairs (precision 8, dfloat = 1)
   int eb = 8;      // bytes per device element (T, or float2 with pairs)
   int ns = 7;      // slices per plane (nf, or 4 pairs)
   int nx = 0, ny = 0, nz = 0, mx = 0, my = 0, mz = 0, px = 0, xoff = 0;
@@ -149,6 +150,9 @@ struct pcgb_box {
   bool dt_known = false;
   KernelHandle kh;
 };
+
+// Element code of the layout kernels: float, double or double-float.
+static int elem_code(const pcgb_box* b) { return b->dfl ? kElemDD : b->tb; }
 
 static void fill_physics(pcgb_box* b) {
   const pcgb_params& p = b->p;
@@ -191,7 +195,14 @@ static int upload_forcing(pcgb_box* b) {
   for (int i = 0; i < b->mx; ++i) { double x = p.xyz0[0] + ((double)(i - 3) + 0.5) * dx; sx[i] = std::sin(p.kf * x); cx[i] = std::cos(p.kf * x); }
   for (int i = 0; i < b->my; ++i) { double y = p.xyz0[1] + ((double)(i - 3) + 0.5) * dy; sy[i] = std::sin(p.kf * y); cy[i] = std::cos(p.kf * y); }
   for (int i = 0; i < b->mz; ++i) { double z = p.xyz0[2] + ((double)(i - 3) + 0.5) * dz; sz[i] = std::sin(p.kf * z); cz[i] = std::cos(p.kf * z); }
-  if (b->tb == 8) {
+  if (b->dfl) {   // double-float pairs: hi = nearest float, lo = nearest float to the rest
+    std::vector<float> hf(2 * n);
+    for (size_t i = 0; i < n; ++i) {
+      hf[2 * i] = (float)h[i];
+      hf[2 * i + 1] = (float)(h[i] - (double)hf[2 * i]);
+    }
+    CK(cudaMemcpyAsync(b->forc, hf.data(), n * 8, cudaMemcpyHostToDevice, g.stream));
+  } else if (b->tb == 8) {
     CK(cudaMemcpyAsync(b->forc, h.data(), n * 8, cudaMemcpyHostToDevice, g.stream));
   } else {
     std::vector<float> hf(n);
@@ -235,7 +246,7 @@ static int set_tiling(pcgb_box* b, int tile, int zd) {
   if ((int)tile_is_pair(b->tb, tile) != b->pairs)
     return set_err(PCGB_E_ARG, "tile %d needs a different device layout than this box was created with", tile);
   TileShape ts = tile_shape(b->tb, tile);
-  KernelHandle kh = get_kernel(b->tb, b->nf, tile);
+  KernelHandle kh = get_kernel(b->tb, b->nf, tile, b->dfl);
   if (!kh.fn) return set_err(PCGB_E_ARG, "no kernel for tile %d", tile);
   if (kh.smem > g.max_smem) return set_err(PCGB_E_UNSUPPORTED, "tile %d needs %d B shared memory", tile, kh.smem);
   b->tile = tile; b->tx = ts.tx; b->ty = ts.ty; b->kh = kh;
@@ -269,6 +280,8 @@ static int validate(const pcgb_params* p) {
   if (!p) return set_err(PCGB_E_ARG, "null parameter block");
   if (p->nx < 3 || p->ny < 3 || p->nz < 3) return set_err(PCGB_E_ARG, "grid %dx%dx%d: each axis needs >= 3 cells", p->nx, p->ny, p->nz);
   if (p->precision != 4 && p->precision != 8) return set_err(PCGB_E_ARG, "precision must be 4 or 8");
+  if (p->dfloat != 0 && p->dfloat != 1) return set_err(PCGB_E_ARG, "dfloat must be 0 or 1");
+  if (p->dfloat && p->precision != 8) return set_err(PCGB_E_ARG, "dfloat needs precision 8 (FP64-class state)");
   if (!(p->Lxyz[0] > 0 && p->Lxyz[1] > 0 && p->Lxyz[2] > 0)) return set_err(PCGB_E_ARG, "Lxyz must be positive");
   if (!(p->cs0 > 0 && p->rho0 > 0 && p->cp > 0 && p->gamma > 0 && p->mu0 > 0))
     return set_err(PCGB_E_ARG, "cs0, rho0, cp, gamma, mu0 must be positive");
@@ -284,6 +297,7 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   b->p = *p;
   b->nf = p->lentropy ? 8 : 7;
   b->tb = p->precision;
+  b->dfl = (p->precision == 8 && p->dfloat) ? 1 : 0;
   b->nx = p->nx; b->ny = p->ny; b->nz = p->nz;
   b->mx = p->nx + 6; b->my = p->ny + 6; b->mz = p->nz + 6;
   {
@@ -357,8 +371,8 @@ extern "C" size_t pcgb_box_bytes(const pcgb_box* b) {
 
 extern "C" int pcgb_box_info(const pcgb_box* b, int* info, int ninfo) {
   if (!b || !info) return set_err(PCGB_E_ARG, "null argument");
-  int v[11] = {b->nx, b->ny, b->nz, b->nf, b->tb, b->tile, b->zd, b->tiles, b->px, b->xoff, b->pairs};
-  for (int i = 0; i < ninfo && i < 11; ++i) info[i] = v[i];
+  int v[12] = {b->nx, b->ny, b->nz, b->nf, b->tb, b->tile, b->zd, b->tiles, b->px, b->xoff, b->pairs, b->dfl};
+  for (int i = 0; i < ninfo && i < 12; ++i) info[i] = v[i];
   return 0;
 }
 
@@ -449,7 +463,7 @@ extern "C" int pcgb_box_load(pcgb_box* b, const double* fh, double t) {
   const long long rows = (long long)b->my * b->mz * b->nf;
   const int in = cur_in(b);
   if (const void* dh = host_alias(fh)) {
-    CK(launch_load_rows(b->tb, b->f[in], static_cast<const double*>(dh), 0, rows, b->mx, b->my, b->mz, b->px,
+    CK(launch_load_rows(elem_code(b), b->f[in], static_cast<const double*>(dh), 0, rows, b->mx, b->my, b->mz, b->px,
                         b->xoff, b->nf, b->pairs, g.stream));
     ++g.launches;
     return box_reset(b, t);
@@ -468,7 +482,7 @@ extern "C" int pcgb_box_load(pcgb_box* b, const double* fh, double t) {
                        g.xfer));
     CK(cudaEventRecord(g.ev_copied[k], g.xfer));
     CK(cudaStreamWaitEvent(g.stream, g.ev_copied[k], 0));
-    CK(launch_load_rows(b->tb, b->f[in], g.stage[k], r0, nr, b->mx, b->my, b->mz, b->px, b->xoff, b->nf, b->pairs,
+    CK(launch_load_rows(elem_code(b), b->f[in], g.stage[k], r0, nr, b->mx, b->my, b->mz, b->px, b->xoff, b->nf, b->pairs,
                         g.stream));
     CK(cudaEventRecord(g.ev_free[k], g.stream));
     ++g.launches;
@@ -495,7 +509,7 @@ extern "C" int pcgb_box_init_field(pcgb_box* b, int field, int kind, double ampl
   char* base = static_cast<char*>(b->f[in]) + (size_t)slice * b->fs * b->eb + (size_t)lane * b->tb;
   const pcgb_params& p = b->p;
   const int comp = (field < 3) ? field : 0;   // ABC component of uu
-  CK(launch_init_field(b->tb, base, kind, kind == 2 ? comp : 0, ampl, a, bb, c, k, seed, b->nx, b->ny, b->nz, b->px,
+  CK(launch_init_field(elem_code(b), base, kind, kind == 2 ? comp : 0, ampl, a, bb, c, k, seed, b->nx, b->ny, b->nz, b->px,
                        b->my, b->xoff, p.xyz0[0], p.xyz0[1], p.xyz0[2], p.Lxyz[0] / p.nx, p.Lxyz[1] / p.ny,
                        p.Lxyz[2] / p.nz, b->pairs ? 2 : 1, g.stream));
   ++g.launches;
@@ -510,7 +524,7 @@ extern "C" int pcgb_box_store(pcgb_box* b, double* fh) {
   // the FP32 carry lives in df between steps (substep counter at a step boundary)
   const void* carry = (b->hdev.comp && (b->nsub % 3) == 0) ? b->df : nullptr;
   if (void* dh = const_cast<void*>(host_alias(fh))) {
-    CK(launch_store_rows(b->tb, static_cast<double*>(dh), b->f[in], carry, 0, rows, b->nx, b->ny, b->nz, b->px,
+    CK(launch_store_rows(elem_code(b), static_cast<double*>(dh), b->f[in], carry, 0, rows, b->nx, b->ny, b->nz, b->px,
                          b->my, b->mz, b->xoff, b->nf, b->pairs, g.stream));
     ++g.launches;
     CK(cudaStreamSynchronize(g.stream));
@@ -525,7 +539,7 @@ extern "C" int pcgb_box_store(pcgb_box* b, double* fh) {
     const int k = c & 1;
     const long long nr = std::min(chunk, rows - r0);
     CK(cudaStreamWaitEvent(g.stream, g.ev_free[k], 0));
-    CK(launch_store_rows(b->tb, g.stage[k], b->f[in], carry, r0, nr, b->nx, b->ny, b->nz, b->px, b->my, b->mz,
+    CK(launch_store_rows(elem_code(b), g.stage[k], b->f[in], carry, r0, nr, b->nx, b->ny, b->nz, b->px, b->my, b->mz,
                          b->xoff, b->nf, b->pairs, g.stream));
     ++g.launches;
     CK(cudaEventRecord(g.ev_copied[k], g.stream));
@@ -631,7 +645,8 @@ extern "C" pcgb_batch* pcgb_batch_create(pcgb_box** boxes, int n, int persistent
   pcgb_batch* B = new pcgb_batch();
   B->boxes.assign(boxes, boxes + n);
   for (auto* b : B->boxes) {
-    if (!b || b->tb != boxes[0]->tb || b->nf != boxes[0]->nf || b->tile != boxes[0]->tile) {
+    if (!b || b->tb != boxes[0]->tb || b->dfl != boxes[0]->dfl || b->nf != boxes[0]->nf ||
+        b->tile != boxes[0]->tile) {
       set_err(PCGB_E_ARG, "a batch needs boxes of one class (precision, fields, tile)");
       delete B;
       return nullptr;
@@ -719,11 +734,11 @@ extern "C" int pcgb_batch_steps(pcgb_batch* B, int nsteps, int use_graph, int gr
 
 // ---------------------------------------------------------------------------
 // autotuner: tile variant and z-sweep depth per (precision, fields, grid)
-static std::map<std::tuple<int, int, int, int, int>, std::tuple<int, int, double>> g_tune;
+static std::map<std::tuple<int, int, int, int, int, int>, std::tuple<int, int, double>> g_tune;
 
 extern "C" int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, double* ms) {
   if (validate(p)) return g_err;
-  auto key = std::make_tuple(p->precision, p->lentropy ? 8 : 7, p->nx, p->ny, p->nz);
+  auto key = std::make_tuple(p->precision, p->dfloat, p->lentropy ? 8 : 7, p->nx, p->ny, p->nz);
   auto it = g_tune.find(key);
   if (it != g_tune.end()) {
     if (tile) *tile = std::get<0>(it->second);
@@ -745,7 +760,7 @@ extern "C" int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, doubl
   if (!b) { cudaEventDestroy(e0); cudaEventDestroy(e1); return g_err; }
   if (bt < 0) { bt = b->tile; bz = b->zd; }
   for (int t = fam * kNumScalarTiles; t < (fam + 1) * kNumScalarTiles && t < ntile; ++t) {
-    KernelHandle kh = get_kernel(b->tb, b->nf, t);
+    KernelHandle kh = get_kernel(b->tb, b->nf, t, b->dfl);
     if (!kh.fn || kh.smem > g.max_smem) continue;
     std::vector<int> zs = {b->nz, 256, 128, 64, 32, 16};
     std::sort(zs.begin(), zs.end());
@@ -910,7 +925,7 @@ extern "C" void loadFarray(void) {
 
 static int box_reload(pcgb_box* b, const pcgb_params& p) {
   if (p.nx != b->p.nx || p.ny != b->p.ny || p.nz != b->p.nz || p.lentropy != b->p.lentropy ||
-      p.precision != b->p.precision)
+      p.precision != b->p.precision || p.dfloat != b->p.dfloat)
     return set_err(PCGB_E_ARG, "reloadConfig cannot change grid, field count or precision");
   b->p = p;
   fill_physics(b);

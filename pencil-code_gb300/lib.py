@@ -35,7 +35,7 @@ class Params(C.Structure):
         ("lohmic_heat", C.c_int), ("lviscosity_heat", C.c_int),
         ("cdt", C.c_double), ("cdtv", C.c_double),
         ("dt", C.c_double), ("dt_mode", C.c_int), ("diag_every", C.c_int),
-        ("tile", C.c_int), ("zdepth", C.c_int),
+        ("tile", C.c_int), ("zdepth", C.c_int), ("dfloat", C.c_int),
     ]
 
     def update(self, **kw) -> "Params":
@@ -270,9 +270,9 @@ class Box:
         return int(load().pcgb_box_bytes(self.h))
 
     def info(self) -> dict:
-        v = (C.c_int * 11)()
-        check(load().pcgb_box_info(self.h, v, 11))
-        keys = ["nx", "ny", "nz", "nf", "bytes_per_value", "tile", "zdepth", "tiles", "px", "xoff", "pairs"]
+        v = (C.c_int * 12)()
+        check(load().pcgb_box_info(self.h, v, 12))
+        keys = ["nx", "ny", "nz", "nf", "bytes_per_value", "tile", "zdepth", "tiles", "px", "xoff", "pairs", "dfloat"]
         return dict(zip(keys, list(v)))
 
 
