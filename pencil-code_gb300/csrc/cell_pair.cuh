@@ -143,6 +143,10 @@ struct PairCell {
 #pragma unroll
         for (int p = 0; p < 4; ++p) dfnext[p] = dfp[p * fs + cidx + ps];
       }
+      if (fl.read_df && z + kDfPrefetch < z1) {
+#pragma unroll
+        for (int p = 0; p < 4; ++p) prefetch_l2(dfp + p * fs + cidx + kDfPrefetch * ps);
+      }
       // gather derivatives pair by pair
       const float2 c0 = st.v(0, 0, 0, 0), c1 = st.v(0, 1, 0, 0), c2 = st.v(0, 2, 0, 0), c3 = st.v(0, 3, 0, 0);
       CellIn<float> c;

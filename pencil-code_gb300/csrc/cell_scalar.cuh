@@ -115,6 +115,10 @@ struct ScalarCell {
 #pragma unroll
         for (int k = 0; k < NF; ++k) dfnext[k] = dfp[k * fs + cidx + ps];
       }
+      if (fl.read_df && z + kDfPrefetch < z1) {
+#pragma unroll
+        for (int k = 0; k < NF; ++k) prefetch_l2(dfp + k * fs + cidx + kDfPrefetch * ps);
+      }
       CellIn<T> c;
 #pragma unroll
       for (int i = 0; i < 3; ++i) {

@@ -10,6 +10,11 @@ namespace pcgb {
 
 enum { MODE_SUBSTEP = 0, MODE_CFL = 1 };
 
+// df of plane z+1 is loaded into registers during plane z; the lines of plane
+// z+kDfPrefetch are requested into L2 so that load finds them there (5 planes
+// ahead measured best on 1024^3: +7 % against no L2 prefetch, 2 ahead +5 %).
+constexpr int kDfPrefetch = 5;
+
 struct LaunchArgs {
   const PcgbBoxDev* boxes;    // [nboxes], sorted by tile0
   int nboxes;

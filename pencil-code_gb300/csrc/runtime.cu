@@ -237,8 +237,8 @@ static int default_zdepth(const pcgb_box* b) {
   return zd;
 }
 
-// FP32: packed pairs on (16,8) tiles, two CTAs per SM; FP64: (32,4)
-static int default_tile(int tb) { return tb == 4 ? 6 : 0; }
+// FP32: packed pairs on (32,8) tiles, one 8-warp CTA per SM; FP64: (32,4)
+static int default_tile(int tb) { return tb == 4 ? 5 : 0; }
 
 static int set_tiling(pcgb_box* b, int tile, int zd) {
   if (tile < 0) tile = default_tile(b->tb);
