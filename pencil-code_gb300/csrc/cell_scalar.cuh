@@ -104,22 +104,8 @@ struct ScalarCell {
       }
     }
 
-    __device__ __forceinline__ void step(const T* const pl[7], int x, int y, int z, int z1, const StepFlags<T>& fl,
-                                         Acc& acc, T& dt1max) {
-      const St st{pl, F};
-      const long long cidx = (long long)(z + 3) * ps + (long long)(y + 3) * px + xoff + x;
-      T dfo[NF];
-#pragma unroll
-      for (int k = 0; k < NF; ++k) dfo[k] = dfnext[k];
-      if (fl.read_df && z + 1 < z1) {
-#pragma unroll
-        for (int k = 0; k < NF; ++k) dfnext[k] = dfp[k * fs + cidx + ps];
-      }
-      if (fl.read_df && z + kDfPrefetch < z1) {
-#pragma unroll
-        for (int k = 0; k < NF; ++k) prefetch_l2(dfp + k * fs + cidx + kDfPrefetch * ps);
-      }
-      CellIn<T> c;
+    // Field values and stencil derivatives of one cell, fully unrolled.
+    static __device__ __forceinline__ void gather(const St& st, CellIn<T>& c, bool want_diag) {
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         c.uu[i] = st.v(0, IUX + i, 0, 0);
@@ -161,9 +147,108 @@ struct ScalarCell {
       c.a1xz = st.derij(IAX + 0, 0, 2); c.a3xz = st.derij(IAX + 2, 0, 2);
       c.a2yz = st.derij(IAX + 1, 1, 2); c.a3yz = st.derij(IAX + 2, 1, 2);
       c.a3xy = c.a2xz = c.a1yz = T(0);
-      if (fl.want_diag) {
+      if (want_diag) {
         c.a3xy = st.derij(IAX + 2, 0, 1); c.a2xz = st.derij(IAX + 1, 0, 2); c.a1yz = st.derij(IAX + 0, 1, 2);
       }
+    }
+
+    // The same stencils and operation order with one copy of each stencil's
+    // code, looped over fields and mixed-derivative jobs; results pass through
+    // thread-local arrays (L1).  Fully unrolled, a double-float plane step is
+    // about 7600 instructions (120 KB of code per z iteration), more than the
+    // instruction caches hold, and its warps stall on instruction fetch.
+    static __device__ __forceinline__ void gather_compact(const St& st, CellIn<T>& c, bool want_diag) {
+      T d1[NF][3], d2[NF][3], m[15];
+#pragma unroll 1
+      for (int k = 0; k < NF; ++k) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) d1[k][j] = st.der(k, j);
+        if (k < ILNRHO || k >= IAX || ENTROPY) {
+#pragma unroll
+          for (int j = 0; j < 3; ++j) d2[k][j] = st.der2(k, j);
+        }
+      }
+      // (field, direction pair) of each mixed derivative; pair 0 = xy, 1 = yz, 2 = xz
+      const int njob = want_diag ? 15 : 12;
+#pragma unroll 1
+      for (int q = 0; q < njob; ++q) {
+        const int code = mixed_job(q);
+        const int k = code >> 2, pr = code & 3;
+        if (pr == 0) m[q] = st.derij(k, 0, 1);
+        else if (pr == 1) m[q] = st.derij(k, 1, 2);
+        else m[q] = st.derij(k, 0, 2);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        c.uu[i] = st.v(0, IUX + i, 0, 0);
+        c.aa[i] = st.v(0, IAX + i, 0, 0);
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+          c.uij[i][jj] = d1[IUX + i][jj];
+          c.aij[i][jj] = d1[IAX + i][jj];
+          c.a2[i][jj] = d2[IAX + i][jj];
+        }
+        c.del2u[i] = (d2[IUX + i][0] + d2[IUX + i][1]) + d2[IUX + i][2];
+      }
+      c.graddivu[0] = (d2[IUX + 0][0] + m[2]) + m[4];
+      c.graddivu[1] = (m[0] + d2[IUX + 1][1]) + m[5];
+      c.graddivu[2] = (m[1] + m[3]) + d2[IUX + 2][2];
+      c.lnrho = st.v(0, ILNRHO, 0, 0);
+#pragma unroll
+      for (int jj = 0; jj < 3; ++jj) c.glnrho[jj] = d1[ILNRHO][jj];
+      if (ENTROPY) {
+        c.ss = st.v(0, ISS, 0, 0);
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) c.gss[jj] = d1[ISS][jj];
+        c.del2lnrho = (d2[ILNRHO][0] + d2[ILNRHO][1]) + d2[ILNRHO][2];
+        c.del2ss = (d2[ISS][0] + d2[ISS][1]) + d2[ISS][2];
+      } else {
+        c.ss = T(0); c.gss[0] = c.gss[1] = c.gss[2] = T(0); c.del2lnrho = c.del2ss = T(0);
+      }
+      c.a1xy = m[6]; c.a2xy = m[7]; c.a1xz = m[8]; c.a3xz = m[9]; c.a2yz = m[10]; c.a3yz = m[11];
+      c.a3xy = c.a2xz = c.a1yz = T(0);
+      if (want_diag) { c.a3xy = m[12]; c.a2xz = m[13]; c.a1yz = m[14]; }
+    }
+
+    // job q of gather_compact: field * 4 + pair (0 xy, 1 yz, 2 xz)
+    static __device__ __forceinline__ int mixed_job(int q) {
+      switch (q) {
+        case 0: return (IUX + 0) * 4 + 0;   // u_x,xy  (grad div u, y)
+        case 1: return (IUX + 0) * 4 + 2;   // u_x,xz  (z)
+        case 2: return (IUX + 1) * 4 + 0;   // u_y,xy  (x)
+        case 3: return (IUX + 1) * 4 + 1;   // u_y,yz  (z)
+        case 4: return (IUX + 2) * 4 + 2;   // u_z,xz  (x)
+        case 5: return (IUX + 2) * 4 + 1;   // u_z,yz  (y)
+        case 6: return (IAX + 0) * 4 + 0;   // A_1,xy
+        case 7: return (IAX + 1) * 4 + 0;   // A_2,xy
+        case 8: return (IAX + 0) * 4 + 2;   // A_1,xz
+        case 9: return (IAX + 2) * 4 + 2;   // A_3,xz
+        case 10: return (IAX + 1) * 4 + 1;  // A_2,yz
+        case 11: return (IAX + 2) * 4 + 1;  // A_3,yz
+        case 12: return (IAX + 2) * 4 + 0;  // A_3,xy (div B only)
+        case 13: return (IAX + 1) * 4 + 2;  // A_2,xz (div B only)
+        default: return (IAX + 0) * 4 + 1;  // A_1,yz (div B only)
+      }
+    }
+
+    __device__ __forceinline__ void step(const T* const pl[7], int x, int y, int z, int z1, const StepFlags<T>& fl,
+                                         Acc& acc, T& dt1max) {
+      const St st{pl, F};
+      const long long cidx = (long long)(z + 3) * ps + (long long)(y + 3) * px + xoff + x;
+      T dfo[NF];
+#pragma unroll
+      for (int k = 0; k < NF; ++k) dfo[k] = dfnext[k];
+      if (fl.read_df && z + 1 < z1) {
+#pragma unroll
+        for (int k = 0; k < NF; ++k) dfnext[k] = dfp[k * fs + cidx + ps];
+      }
+      if (fl.read_df && z + kDfPrefetch < z1) {
+#pragma unroll
+        for (int k = 0; k < NF; ++k) prefetch_l2(dfp + k * fs + cidx + kDfPrefetch * ps);
+      }
+      CellIn<T> c;
+      if constexpr (is_dd<T>::value) gather_compact(st, c, fl.want_diag);
+      else gather(st, c, fl.want_diag);
       T fc[3] = {T(0), T(0), T(0)};
       if (forcing) {   // forcing_cont 'ABC', forcing.f90:5894-5896
         fc[0] = P.fact * (P.abc_c * fsz + (P.fact2 * P.abc_b) * fcy);

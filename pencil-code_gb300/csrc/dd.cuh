@@ -28,6 +28,11 @@ struct __align__(8) dd {
   __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
 };
 
+template <typename T>
+struct is_dd { static constexpr bool value = false; };
+template <>
+struct is_dd<dd> { static constexpr bool value = true; };
+
 // s + e == a + b exactly (round-to-nearest; the _rn intrinsics keep the
 // compiler from contracting or reordering)
 __device__ __forceinline__ void dd_two_sum(float a, float b, float& s, float& e) {
