@@ -423,7 +423,7 @@ def run_serve(args):
     res = []
     for rate in args.rates:
         reqs = serve.draw_requests(args.requests, seed=args.seed, steps_scale=args.steps_scale,
-                                   fp64_fraction=args.fp64_fraction)
+                                   fp64_fraction=args.fp64_fraction, fp64_dfloat=not args.fp64_native)
         row = {"rate": rate}
         for mode, maxa in (("batched", 1 << 20), ("fifo", 1)):
             row[mode] = serve.run_stream(reqs, rate, seed=args.seed, max_active=maxa, budget=args.budget_gb * 1e9,
@@ -433,6 +433,7 @@ def run_serve(args):
             "data": "synthetic Poisson request stream",
             "config": {"requests": args.requests, "sizes": "{32,64,128,256}^3 weights .4/.3/.2/.1",
                        "physics": "isothermal or entropy p=0.5", "fp64_fraction": args.fp64_fraction,
+                       "fp64_state": "native FP64" if args.fp64_native else "double-float (FP64 parity bar)",
                        "steps": f"U[100,2000] x {args.steps_scale}", "budget_gb": args.budget_gb,
                        "round_steps": args.round_steps},
             "results": res}
@@ -466,6 +467,7 @@ def main():
     ap.add_argument("--rates", type=float, nargs="+", default=[5.0, 50.0])
     ap.add_argument("--steps-scale", type=float, default=0.1)
     ap.add_argument("--fp64-fraction", type=float, default=0.5)
+    ap.add_argument("--fp64-native", action="store_true", help="serve FP64 requests with native FP64 state")
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--round-steps", type=int, default=10)
     args = ap.parse_args()

@@ -11,7 +11,9 @@ pytestmark = pytest.mark.gpu
 
 
 def _req(pc, n, prec, ent, seed, nu, k):
-    p = pc.default_params(nx=n, ny=n, nz=n, lentropy=int(ent), gamma=5.0 / 3.0 if ent else 1.0, precision=prec,
+    """prec: 4 FP32, 8 FP64, 9 FP64-class double-float."""
+    p = pc.default_params(nx=n, ny=n, nz=n, lentropy=int(ent), gamma=5.0 / 3.0 if ent else 1.0,
+                          precision=4 if prec == 4 else 8, dfloat=int(prec == 9),
                           comp=1, nu=nu, eta=1.3 * nu, chi=nu if ent else 0.0, lforcing_cont=1, ampl_ff=0.03, kf=k,
                           dt=0.0, dt_mode=1, cdt=0.4)
     return p
@@ -32,7 +34,8 @@ def test_mix_equals_alone(pc):
     serve = importlib.import_module("pencil-code_gb300.serve")
     ens = importlib.import_module("pencil-code_gb300.ensemble")
     specs = [(32, 4, False, 11, 2e-3, 1.0, 7), (48, 8, False, 12, 5e-3, 2.0, 5), (32, 4, True, 13, 3e-3, 3.0, 9),
-             (64, 4, False, 14, 1e-3, 2.0, 4), (16, 8, True, 15, 8e-3, 1.0, 6), (40, 4, False, 16, 4e-3, 1.0, 8)]
+             (64, 4, False, 14, 1e-3, 2.0, 4), (16, 8, True, 15, 8e-3, 1.0, 6), (40, 4, False, 16, 4e-3, 1.0, 8),
+             (32, 9, False, 17, 2e-3, 2.0, 5), (24, 9, True, 18, 6e-3, 1.0, 7)]
     srv = serve.Server(budget_bytes=20e9, round_steps=3)
     outs, ids = [], []
     for n, prec, ent, seed, nu, k, steps in specs:
