@@ -10,7 +10,9 @@ namespace pcgb {
 // Tile variants.  Ids 0..3 use the field-major layout (one value per field per
 // cell); for FP32, ids 4..7 use the packed field-pair layout (cell_pair.cuh).
 //   FP32: 0 (32,4)x2  1 (32,8)  2 (16,8)x2  3 (64,4)  4 pair(32,4)x2  5 pair(32,8)  6 pair(16,8)x2  7 pair(64,4)
-//   FP64 and double-float: 0 (32,4)  1 (16,8)  2 (16,4)  3 (32,2)
+//   FP64 and double-float: 0 (32,4)  1 (16,8)  2 (24,8)  3 (32,6)
+// (FP64-family rings of 8 planes x 7 or 8 fields fit one CTA per SM; the
+// 192-thread tiles 2 and 3 give 6 warps per SM instead of 4.)
 // "x2" variants ask for two resident CTAs per SM.
 struct TileShape { int tx, ty; };
 constexpr int kNumScalarTiles = 4;
@@ -19,7 +21,7 @@ inline int num_tiles(int dtype_bytes) { return dtype_bytes == 4 ? kNumTiles : kN
 inline bool tile_is_pair(int dtype_bytes, int tile) { return dtype_bytes == 4 && tile >= kNumScalarTiles; }
 inline TileShape tile_shape(int dtype_bytes, int tile) {
   static const TileShape f32[kNumScalarTiles] = {{32, 4}, {32, 8}, {16, 8}, {64, 4}};
-  static const TileShape f64[kNumScalarTiles] = {{32, 4}, {16, 8}, {16, 4}, {32, 2}};
+  static const TileShape f64[kNumScalarTiles] = {{32, 4}, {16, 8}, {24, 8}, {32, 6}};
   return dtype_bytes == 4 ? f32[tile % kNumScalarTiles] : f64[tile];
 }
 
@@ -80,8 +82,8 @@ static KernelHandle make_kernel_handle() {
         switch (tile) {                                                                            \
           case 0: cache[0] = make_kernel_handle<ScalarCell<T, NF, 32, 4>, 32, 4, 8, 1>(); break;   \
           case 1: cache[1] = make_kernel_handle<ScalarCell<T, NF, 16, 8>, 16, 8, 8, 1>(); break;   \
-          case 2: cache[2] = make_kernel_handle<ScalarCell<T, NF, 16, 4>, 16, 4, 8, 1>(); break;   \
-          default: cache[3] = make_kernel_handle<ScalarCell<T, NF, 32, 2>, 32, 2, 8, 1>(); break;  \
+          case 2: cache[2] = make_kernel_handle<ScalarCell<T, NF, 24, 8>, 24, 8, 8, 1>(); break;   \
+          default: cache[3] = make_kernel_handle<ScalarCell<T, NF, 32, 6>, 32, 6, 8, 1>(); break;  \
         }                                                                                          \
       }                                                                                            \
       init[tile] = true;                                                                           \

@@ -237,11 +237,13 @@ static int default_zdepth(const pcgb_box* b) {
   return zd;
 }
 
-// FP32: packed pairs on (32,8) tiles, one 8-warp CTA per SM; FP64: (32,4)
-static int default_tile(int tb) { return tb == 4 ? 5 : 0; }
+// FP32: packed pairs on (32,8) tiles, one 8-warp CTA per SM; FP64 and
+// double-float: one 6-warp CTA per SM, (32,6) with 7 fields, (24,8) with 8
+// (an 8-field ring of (32,6) planes needs 246 KB of shared memory)
+static int default_tile(int tb, int nf) { return tb == 4 ? 5 : (nf == 8 ? 2 : 3); }
 
 static int set_tiling(pcgb_box* b, int tile, int zd) {
-  if (tile < 0) tile = default_tile(b->tb);
+  if (tile < 0) tile = default_tile(b->tb, b->nf);
   if (tile >= num_tiles(b->tb)) return set_err(PCGB_E_ARG, "tile variant %d out of range", tile);
   if ((int)tile_is_pair(b->tb, tile) != b->pairs)
     return set_err(PCGB_E_ARG, "tile %d needs a different device layout than this box was created with", tile);
@@ -301,7 +303,7 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   b->nx = p->nx; b->ny = p->ny; b->nz = p->nz;
   b->mx = p->nx + 6; b->my = p->ny + 6; b->mz = p->nz + 6;
   {
-    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb);
+    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb, b->nf);
     b->pairs = (t0 < num_tiles(b->tb) && tile_is_pair(b->tb, t0)) ? 1 : 0;
   }
   b->eb = b->pairs ? 8 : b->tb;
@@ -351,7 +353,7 @@ extern "C" void pcgb_box_destroy(pcgb_box* b) {
 extern "C" size_t pcgb_params_bytes(const pcgb_params* p) {
   if (!p || p->nx < 1 || p->ny < 1 || p->nz < 1 || (p->precision != 4 && p->precision != 8)) return 0;
   const int tb = p->precision, nf = p->lentropy ? 8 : 7;
-  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb);
+  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb, nf);
   const int pairs = (t0 < num_tiles(tb) && tile_is_pair(tb, t0)) ? 1 : 0;
   const int eb = pairs ? 8 : tb, ns = pairs ? 4 : nf;
   const int xoff = 128 / eb;
