@@ -45,7 +45,7 @@ typedef double REAL_PCGB; /* REAL of the double build */
  *   &run_pars dt, cdt, cdtv (cdata.f90:235-239).
  * ------------------------------------------------------------------------- */
 typedef struct pcgb_params {
-  int nx, ny, nz;          /* nxgrid, nygrid, nzgrid */
+  int nx, ny, nz;          /* nxgrid, nygrid, nzgrid; each >= 6 */
   int lentropy;            /* 0: ENTROPY=noentropy (7 fields), 1: entropy (8 fields) */
   int precision;           /* device state: 8 = FP64, 4 = FP32 */
   int comp;                /* FP32 only: compensated 2N accumulation (1 = on) */

@@ -124,6 +124,8 @@ struct StepFlags {
 
 // Periodic images of an interior index: the index itself and, near a face,
 // its copy in the ghost zone on the opposite side (boundcond.f90:2387-2531).
+// With n >= 6 cells on the axis an index has at most one ghost image (the
+// runtime rejects smaller grids).
 struct Images {
   int v[2];
   int n;

@@ -66,8 +66,8 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
     return fail(2, "invalid argument");
   if (p->precision != 4 && p->precision != 8) return fail(2, "precision must be 4 or 8");
   if (p->dfloat) return fail(2, "double-float state is not available here (use the box API)");
-  if (p->nx < 3 || p->ny < 3 || p->nz < 3 || p->nx > kMaxExtent || p->ny > kMaxExtent || p->nz > kMaxExtent)
-    return fail(7, "grid extent outside [3, PCGB_NOALLOC_MAX_EXTENT]");
+  if (p->nx < 6 || p->ny < 6 || p->nz < 6 || p->nx > kMaxExtent || p->ny > kMaxExtent || p->nz > kMaxExtent)
+    return fail(7, "grid extent outside [6, PCGB_NOALLOC_MAX_EXTENT]");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   // set-up once per device, with the device current

@@ -280,7 +280,10 @@ static void box_free(pcgb_box* b) {
 
 static int validate(const pcgb_params* p) {
   if (!p) return set_err(PCGB_E_ARG, "null parameter block");
-  if (p->nx < 3 || p->ny < 3 || p->nz < 3) return set_err(PCGB_E_ARG, "grid %dx%dx%d: each axis needs >= 3 cells", p->nx, p->ny, p->nz);
+  // >= 2 x nghost cells: the substep kernel writes each cell's periodic ghost
+  // image on one side of an axis (Images in mhd_common.cuh)
+  if (p->nx < 6 || p->ny < 6 || p->nz < 6)
+    return set_err(PCGB_E_ARG, "grid %dx%dx%d: each axis needs >= 6 cells", p->nx, p->ny, p->nz);
   if (p->precision != 4 && p->precision != 8) return set_err(PCGB_E_ARG, "precision must be 4 or 8");
   if (p->dfloat != 0 && p->dfloat != 1) return set_err(PCGB_E_ARG, "dfloat must be 0 or 1");
   if (p->dfloat && p->precision != 8) return set_err(PCGB_E_ARG, "dfloat needs precision 8 (FP64-class state)");

@@ -98,7 +98,8 @@ def test_no_cpu_fallback_without_gpu(pc):
 
 def test_parameter_validation(pc):
     L = pc.load()
-    for bad in (dict(nx=2), dict(precision=2), dict(cdt=0.0), dict(cs0=-1.0), dict(dt=-1.0)):
+    for bad in (dict(nx=2), dict(nx=5), dict(nz=4), dict(precision=2), dict(cdt=0.0), dict(cs0=-1.0),
+                dict(dt=-1.0), dict(precision=4, dfloat=1), dict(dfloat=2)):
         p = pc.default_params(**bad)
         assert L.pcgb_set_params(C.byref(p)) != 0, bad
 

@@ -233,3 +233,25 @@ def test_fp32_pair_layout_diagnostics_and_cfl(pc, ic, orc):
     assert abs(dt * dt1 - 1.0) <= 1e-6
     for k in (orc.D_U2SUM, orc.D_B2SUM, orc.D_EKINSUM, orc.D_RHOSUM, orc.D_J2SUM):
         assert abs(raw[k + 1] - dg[k]) <= 1e-5 * abs(dg[k]), k
+
+
+@pytest.mark.parametrize("n", [(37, 19, 11), (6, 6, 6), (6, 40, 7)])
+@pytest.mark.parametrize("mode", ["f64", "dfloat", "f32pair", "f32"])
+def test_ragged_and_minimal_grids(pc, ic, orc, n, mode):
+    """Grids that are not multiples of any tile, and the smallest grid the
+    periodic ghost images allow (6 cells per axis), in every state mode."""
+    kw = dict(f64=dict(precision=8), dfloat=dict(precision=8, dfloat=1),
+              f32pair=dict(precision=4, comp=1, tile=5), f32=dict(precision=4, comp=1, tile=0))[mode]
+    p = pc.default_params(nx=n[0], ny=n[1], nz=n[2], gamma=1.0, nu=1e-2, eta=1e-2, dt=2e-3,
+                          lforcing_cont=1, ampl_ff=0.02, kf=1.0, b_ext=(0.0, 0.05, 0.0), **kw)
+    p.update(Lxyz=(0.37 * np.pi, 0.19 * np.pi, 0.11 * np.pi) if n[0] == 37 else (2 * np.pi,) * 3)
+    f0 = iso_state(pc, ic, p, ampl=1e-2, seed=21)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(5)
+    g = box.store()
+    ref, _, _ = run_oracle(orc, p, f0, 5)
+    tol = TOL32 if mode.startswith("f32") else TOL64
+    err = rel_err(g, ref, LOG7 if mode.startswith("f32") else ())
+    assert np.all(err <= tol), err
+    assert np.array_equal(ic.fill_ghosts(g.copy()), g)
