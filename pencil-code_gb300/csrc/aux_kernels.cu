@@ -98,6 +98,37 @@ __global__ void store_rows_kernel(double* __restrict__ stage, const T* __restric
   }
 }
 
+// Double-float pair layout: device element e of 16 bytes holds (hi_a, hi_b,
+// lo_a, lo_b); dev_index's pair index 2e + lane selects the field.
+__global__ void load_rows_ddpair_kernel(float* __restrict__ f, const double* __restrict__ stage, long long r0,
+                                        long long nr, int mx, int my, int mz, int px, int xoff, int nf) {
+  const long long total = nr * mx;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long r = q / mx;
+    const int i = (int)(q - r * mx);
+    const long long pi = dev_index(r0 + r, i, my, mz, px, xoff, nf, 1);
+    const long long e = pi >> 1, lane = pi & 1;
+    const dd v(stage[q]);
+    f[4 * e + lane] = v.hi;
+    f[4 * e + 2 + lane] = v.lo;
+  }
+}
+
+__global__ void store_rows_ddpair_kernel(double* __restrict__ stage, const float* __restrict__ f, long long r0,
+                                         long long nr, int nx, int my, int mz, int px, int xoff, int nf) {
+  const int mx = nx + 6;
+  const long long total = nr * mx;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long r = q / mx;
+    const int i = (int)(q - r * mx);
+    const long long pi = dev_index(r0 + r, i, my, mz, px, xoff, nf, 1);
+    const long long e = pi >> 1, lane = pi & 1;
+    stage[q] = (double)f[4 * e + lane] + (double)f[4 * e + 2 + lane];
+  }
+}
+
 static int grid_for(long long n, int threads) {
   long long g = (n + threads - 1) / threads;
   if (g > 65535LL * 16) g = 65535LL * 16;
@@ -111,6 +142,8 @@ cudaError_t launch_ghost_fill(int tbytes, void* f, int nx, int ny, int nz, int p
   const int th = 256, g = grid_for(n, th);
   if (tbytes == 4)
     ghost_fill_kernel<float><<<g, th, 0, s>>>((float*)f, nx, ny, nz, px, my, mz, xoff, nf);
+  else if (tbytes == 16)
+    ghost_fill_kernel<float4><<<g, th, 0, s>>>((float4*)f, nx, ny, nz, px, my, mz, xoff, nf);
   else
     ghost_fill_kernel<double><<<g, th, 0, s>>>((double*)f, nx, ny, nz, px, my, mz, xoff, nf);
   return cudaGetLastError();
@@ -123,6 +156,8 @@ cudaError_t launch_load_rows(int tbytes, void* f, const double* stage, long long
     load_rows_kernel<float><<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
   else if (tbytes == kElemDD)
     load_rows_kernel<dd><<<g, th, 0, s>>>((dd*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
+  else if (tbytes == kElemDDPair)
+    load_rows_ddpair_kernel<<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, my, mz, px, xoff, nf);
   else
     load_rows_kernel<double><<<g, th, 0, s>>>((double*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
   return cudaGetLastError();
@@ -138,6 +173,8 @@ cudaError_t launch_store_rows(int tbytes, double* stage, const void* f, const vo
   else if (tbytes == kElemDD)
     store_rows_kernel<dd><<<g, th, 0, s>>>(stage, (const dd*)f, nullptr, r0, nr, nx, ny, nz, px, my, mz, xoff, nf,
                                            pairs);
+  else if (tbytes == kElemDDPair)
+    store_rows_ddpair_kernel<<<g, th, 0, s>>>(stage, (const float*)f, r0, nr, nx, my, mz, px, xoff, nf);
   else
     store_rows_kernel<double><<<g, th, 0, s>>>(stage, (const double*)f, (const double*)carry, r0, nr, nx, ny, nz, px,
                                                my, mz, xoff, nf, pairs);
@@ -160,10 +197,30 @@ __device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
 // kind 0: set to zero; 1: add ampl * N(0,1) (Box-Muller on two counter-based
 // uniforms); 2: add the ABC flow component fld (hydro.f90:2214-2220) with
 // amplitudes a,b,c and wavenumber k on the cell-centred grid.
+// Value access of init_field_kernel: element e of a T array with a stride
+// (field-major, or one lane of the FP32 pair layout), or one field of the
+// double-float pair layout (hi at float 4e, lo at float 4e + 2 of a lane base).
 template <typename T>
-__global__ void init_field_kernel(T* __restrict__ f, int kind, int comp, double ampl, double a, double b, double c,
-                                  double k, unsigned long long seed, int nx, int ny, int nz, int px, int my, int xoff,
-                                  double x0, double y0, double z0, double dx, double dy, double dz, int estride) {
+struct ElemRef {
+  T* f;
+  int stride;
+  __device__ __forceinline__ double get(long long e) const { return (double)f[stride * e]; }
+  __device__ __forceinline__ void set(long long e, double v) const { f[stride * e] = (T)v; }
+};
+struct DDPairRef {
+  float* f;
+  __device__ __forceinline__ double get(long long e) const { return (double)f[4 * e] + (double)f[4 * e + 2]; }
+  __device__ __forceinline__ void set(long long e, double v) const {
+    const dd d(v);
+    f[4 * e] = d.hi;
+    f[4 * e + 2] = d.lo;
+  }
+};
+
+template <class REF>
+__global__ void init_field_kernel(REF f, int kind, int comp, double ampl, double a, double b, double c, double k,
+                                  unsigned long long seed, int nx, int ny, int nz, int px, int my, int xoff, double x0,
+                                  double y0, double z0, double dx, double dy, double dz) {
   const long long total = (long long)nx * ny * nz;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
@@ -171,23 +228,23 @@ __global__ void init_field_kernel(T* __restrict__ f, int kind, int comp, double 
     const long long r = q / nx;
     const int j = (int)(r % ny);
     const int kk = (int)(r / ny);
-    const long long idx = estride * ((long long)(kk + 3) * px * my + (long long)(j + 3) * px + xoff + i);
+    const long long idx = (long long)(kk + 3) * px * my + (long long)(j + 3) * px + xoff + i;
     if (kind == 0) {
-      f[idx] = T(0);
+      f.set(idx, 0.0);
     } else if (kind == 1) {
       const unsigned long long h1 = splitmix64(seed * 0x100000001B3ull + 2ull * (unsigned long long)q);
       const unsigned long long h2 = splitmix64(h1 ^ 0xD1B54A32D192ED03ull);
       const double u1 = ((double)(h1 >> 11) + 1.0) * (1.0 / 9007199254740993.0);   // (0,1]
       const double u2 = (double)(h2 >> 11) * (1.0 / 9007199254740992.0);            // [0,1)
       const double g = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
-      f[idx] = (T)((double)f[idx] + ampl * g);
+      f.set(idx, f.get(idx) + ampl * g);
     } else {
       const double x = x0 + ((double)i + 0.5) * dx, y = y0 + ((double)j + 0.5) * dy, z = z0 + ((double)kk + 0.5) * dz;
       double v;
       if (comp == 0) v = a * sin(k * z) + c * cos(k * y);
       else if (comp == 1) v = b * sin(k * x) + a * cos(k * z);
       else v = c * sin(k * y) + b * cos(k * x);
-      f[idx] = (T)((double)f[idx] + ampl * v);
+      f.set(idx, f.get(idx) + ampl * v);
     }
   }
 }
@@ -198,14 +255,17 @@ cudaError_t launch_init_field(int tbytes, void* f, int kind, int comp, double am
                               cudaStream_t s) {
   const int th = 256, g = grid_for((long long)nx * ny * nz, th);
   if (tbytes == 4)
-    init_field_kernel<float><<<g, th, 0, s>>>((float*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my, xoff,
-                                              x0, y0, z0, dx, dy, dz, estride);
+    init_field_kernel<<<g, th, 0, s>>>(ElemRef<float>{(float*)f, estride}, kind, comp, ampl, a, b, c, k, seed, nx, ny,
+                                       nz, px, my, xoff, x0, y0, z0, dx, dy, dz);
   else if (tbytes == kElemDD)
-    init_field_kernel<dd><<<g, th, 0, s>>>((dd*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my, xoff, x0,
-                                           y0, z0, dx, dy, dz, estride);
+    init_field_kernel<<<g, th, 0, s>>>(ElemRef<dd>{(dd*)f, estride}, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz,
+                                       px, my, xoff, x0, y0, z0, dx, dy, dz);
+  else if (tbytes == kElemDDPair)
+    init_field_kernel<<<g, th, 0, s>>>(DDPairRef{(float*)f}, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my,
+                                       xoff, x0, y0, z0, dx, dy, dz);
   else
-    init_field_kernel<double><<<g, th, 0, s>>>((double*)f, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my,
-                                               xoff, x0, y0, z0, dx, dy, dz, estride);
+    init_field_kernel<<<g, th, 0, s>>>(ElemRef<double>{(double*)f, estride}, kind, comp, ampl, a, b, c, k, seed, nx,
+                                       ny, nz, px, my, xoff, x0, y0, z0, dx, dy, dz);
   return cudaGetLastError();
 }
 

@@ -3,9 +3,12 @@
 #include <cuda_runtime.h>
 
 namespace pcgb {
-// Element codes passed as `tbytes`: 4 float, 8 double, kElemDD double-float
-// (an 8-byte hi/lo pair of floats, dd.cuh).
+// Element codes passed as `tbytes` to the row and init kernels: 4 float,
+// 8 double, kElemDD double-float (an 8-byte hi/lo pair of floats, dd.cuh),
+// kElemDDPair two double-float fields packed as one 16-byte dd2 (lanes as in
+// the FP32 pair layout).  launch_ghost_fill takes the element size in bytes.
 constexpr int kElemDD = 16;
+constexpr int kElemDDPair = 32;
 cudaError_t launch_ghost_fill(int tbytes, void* f, int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf,
                               cudaStream_t s);
 // pairs = 1: packed field-pair layout (P0=(ux,ax) P1=(uy,ay) P2=(uz,az) P3=(lnrho,ss)), px/xoff in pair units

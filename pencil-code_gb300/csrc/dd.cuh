@@ -93,6 +93,66 @@ __device__ __forceinline__ dd texp(dd v) { return dd(exp((double)v)); }
 __device__ __forceinline__ dd tsqrt(dd v) { return dd(sqrt((double)v)); }
 __device__ __forceinline__ dd tabs(dd v) { return v.hi < 0.f ? -v : v; }
 
+// Two double-float values in one 16-byte element, hi = (a.hi, b.hi) and
+// lo = (a.lo, b.lo): the algorithms above run on both at once with packed
+// f32x2 instructions (FADD2/FMUL2/FFMA2), lane by lane the same operations,
+// so each lane's result equals the scalar dd result bit for bit.
+struct __align__(16) dd2 {
+  float2 hi, lo;
+};
+
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+__device__ __forceinline__ void dd2_two_sum(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  const float2 bb = __fadd2_rn(s, f2neg(a));
+  e = __fadd2_rn(__fadd2_rn(a, f2neg(__fadd2_rn(s, f2neg(bb)))), __fadd2_rn(b, f2neg(bb)));
+}
+
+__device__ __forceinline__ void dd2_fast_two_sum(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  e = __fadd2_rn(b, f2neg(__fadd2_rn(s, f2neg(a))));
+}
+
+__device__ __forceinline__ dd2 operator+(dd2 x, dd2 y) {
+  float2 sh, sl;
+  dd2_two_sum(x.hi, y.hi, sh, sl);
+  const float2 w = __fadd2_rn(sl, __fadd2_rn(x.lo, y.lo));
+  dd2 z;
+  dd2_fast_two_sum(sh, w, z.hi, z.lo);
+  return z;
+}
+
+__device__ __forceinline__ dd2 operator-(dd2 x) { return dd2{f2neg(x.hi), f2neg(x.lo)}; }
+__device__ __forceinline__ dd2 operator-(dd2 x, dd2 y) { return x + dd2{f2neg(y.hi), f2neg(y.lo)}; }
+
+__device__ __forceinline__ dd2 operator*(dd2 x, dd2 y) {
+  const float2 ch = __fmul2_rn(x.hi, y.hi);
+  const float2 cl1 = __ffma2_rn(x.hi, y.hi, f2neg(ch));
+  const float2 tl0 = __fmul2_rn(x.lo, y.lo);
+  const float2 tl1 = __ffma2_rn(x.hi, y.lo, tl0);
+  const float2 cl2 = __ffma2_rn(x.lo, y.hi, tl1);
+  const float2 cl3 = __fadd2_rn(cl1, cl2);
+  dd2 z;
+  dd2_fast_two_sum(ch, cl3, z.hi, z.lo);
+  return z;
+}
+
+__device__ __forceinline__ dd2 dd2_scale(dd2 x, float c) {
+  const float2 cc = make_float2(c, c);
+  const float2 ch = __fmul2_rn(x.hi, cc);
+  const float2 cl1 = __ffma2_rn(x.hi, cc, f2neg(ch));
+  const float2 cl3 = __ffma2_rn(x.lo, cc, cl1);
+  dd2 z;
+  dd2_fast_two_sum(ch, cl3, z.hi, z.lo);
+  return z;
+}
+
+__device__ __forceinline__ dd2 dd2_splat(dd v) { return dd2{make_float2(v.hi, v.hi), make_float2(v.lo, v.lo)}; }
+__device__ __forceinline__ dd dd2_lane0(dd2 x) { return dd(x.hi.x, x.lo.x); }
+__device__ __forceinline__ dd dd2_lane1(dd2 x) { return dd(x.hi.y, x.lo.y); }
+__device__ __forceinline__ dd2 dd2_pack(dd a, dd b) { return dd2{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)}; }
+
 // Weight times value: the FP32/FP64 paths multiply by T(c); double-float
 // values use the cheaper product with an exact FP32 weight.
 template <typename T>

@@ -1,6 +1,7 @@
 // kernels.cuh -- host-side view of the compiled substep kernel variants.
 #pragma once
 #include <cuda_runtime.h>
+#include "cell_ddpair.cuh"
 #include "cell_pair.cuh"
 #include "cell_scalar.cuh"
 #include "mhd_driver.cuh"
@@ -8,21 +9,29 @@
 namespace pcgb {
 
 // Tile variants.  Ids 0..3 use the field-major layout (one value per field per
-// cell); for FP32, ids 4..7 use the packed field-pair layout (cell_pair.cuh).
+// cell); for FP32 and double-float, ids 4..7 use the packed field-pair layout
+// (cell_pair.cuh: float2 elements; cell_ddpair.cuh: 16-byte dd2 elements).
 //   FP32: 0 (32,4)x2  1 (32,8)  2 (16,8)x2  3 (64,4)  4 pair(32,4)x2  5 pair(32,8)  6 pair(16,8)x2  7 pair(64,4)
-//   FP64 and double-float: 0 (32,4)  1 (16,8)  2 (24,8)  3 (32,6)
-// (FP64-family rings of 8 planes x 7 or 8 fields fit one CTA per SM; the
-// 192-thread tiles 2 and 3 give 6 warps per SM instead of 4.)
-// "x2" variants ask for two resident CTAs per SM.
+//   FP64: 0 (32,4)  1 (16,8)  2 (24,8)  3 (32,6)
+//   double-float: 0..3 as FP64, 4 pair(24,8)  5 pair(16,12)  6 pair(16,8)  7 pair(32,4)
+// (FP64-family rings of 8 planes fit one CTA per SM; the 192-thread tiles
+// give 6 warps per SM instead of 4.)  "x2" variants ask for two resident CTAs per SM.
+// dfl: the box holds the double-float state.
 struct TileShape { int tx, ty; };
 constexpr int kNumScalarTiles = 4;
 constexpr int kNumTiles = 8;
-inline int num_tiles(int dtype_bytes) { return dtype_bytes == 4 ? kNumTiles : kNumScalarTiles; }
-inline bool tile_is_pair(int dtype_bytes, int tile) { return dtype_bytes == 4 && tile >= kNumScalarTiles; }
-inline TileShape tile_shape(int dtype_bytes, int tile) {
+inline int num_tiles(int dtype_bytes, int dfl = 0) {
+  return (dtype_bytes == 4 || dfl) ? kNumTiles : kNumScalarTiles;
+}
+inline bool tile_is_pair(int dtype_bytes, int tile, int dfl = 0) {
+  return (dtype_bytes == 4 || dfl) && tile >= kNumScalarTiles;
+}
+inline TileShape tile_shape(int dtype_bytes, int tile, int dfl = 0) {
   static const TileShape f32[kNumScalarTiles] = {{32, 4}, {32, 8}, {16, 8}, {64, 4}};
   static const TileShape f64[kNumScalarTiles] = {{32, 4}, {16, 8}, {24, 8}, {32, 6}};
-  return dtype_bytes == 4 ? f32[tile % kNumScalarTiles] : f64[tile];
+  static const TileShape ddp[kNumScalarTiles] = {{24, 8}, {16, 12}, {16, 8}, {32, 4}};
+  if (dtype_bytes == 4) return f32[tile % kNumScalarTiles];
+  return (dfl && tile >= kNumScalarTiles) ? ddp[tile - kNumScalarTiles] : f64[tile % kNumScalarTiles];
 }
 
 struct KernelHandle {
@@ -47,6 +56,16 @@ inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile, int dfl = 0) {
 }
 
 template <class CELL, int TX, int TY, int R, int MB>
+static KernelHandle make_kernel_handle();
+
+// Pair tiles of the double-float family (no kernel for the other element types).
+template <typename T, int NF, int TX, int TY>
+static KernelHandle make_dd_pair_handle() {
+  if constexpr (is_dd<T>::value) return make_kernel_handle<DDPairCell<NF, TX, TY>, TX, TY, 8, 1>();
+  else return KernelHandle();
+}
+
+template <class CELL, int TX, int TY, int R, int MB>
 static KernelHandle make_kernel_handle() {
   KernelHandle h;
   h.fn = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB>);
@@ -65,7 +84,7 @@ static KernelHandle make_kernel_handle() {
   KernelHandle NAME(int tile) {                                                                    \
     static KernelHandle cache[kNumTiles];                                                          \
     static bool init[kNumTiles] = {false, false, false, false, false, false, false, false};        \
-    if (tile < 0 || tile >= num_tiles(sizeof(T))) return KernelHandle();                           \
+    if (tile < 0 || tile >= num_tiles(sizeof(T), is_dd<T>::value)) return KernelHandle();          \
     if (!init[tile]) {                                                                             \
       if constexpr (sizeof(T) == 4) {                                                              \
         switch (tile) {                                                                            \
@@ -80,6 +99,10 @@ static KernelHandle make_kernel_handle() {
         }                                                                                          \
       } else {                                                                                     \
         switch (tile) {                                                                            \
+          case 4: cache[4] = make_dd_pair_handle<T, NF, 24, 8>(); break;                           \
+          case 5: cache[5] = make_dd_pair_handle<T, NF, 16, 12>(); break;                          \
+          case 6: cache[6] = make_dd_pair_handle<T, NF, 16, 8>(); break;                           \
+          case 7: cache[7] = make_dd_pair_handle<T, NF, 32, 4>(); break;                           \
           case 0: cache[0] = make_kernel_handle<ScalarCell<T, NF, 32, 4>, 32, 4, 8, 1>(); break;   \
           case 1: cache[1] = make_kernel_handle<ScalarCell<T, NF, 16, 8>, 16, 8, 8, 1>(); break;   \
           case 2: cache[2] = make_kernel_handle<ScalarCell<T, NF, 24, 8>, 24, 8, 8, 1>(); break;   \

@@ -137,7 +137,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
     const unsigned int sbase = gplane % RING, pbase = gplane / RING;
     // producer: prologue (TMA box origin held in a register: stores through the
     // cell's output pointers would otherwise force a reload from the descriptor)
-    const int tma_x = B.xoff + x0 - 4;
+    // (16-byte dd2 elements travel as two 8-byte TMA elements)
+    const int tma_x = (B.xoff + x0 - 4) * (sizeof(Elem) == 16 ? 2 : 1);
     if (tid == 0) {
       prefetch_tensormap(tmap);
       const int npro = nplanes < RING ? nplanes : RING;

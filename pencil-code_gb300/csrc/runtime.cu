@@ -152,7 +152,7 @@ struct pcgb_box {
 };
 
 // Element code of the layout kernels: float, double or double-float.
-static int elem_code(const pcgb_box* b) { return b->dfl ? kElemDD : b->tb; }
+static int elem_code(const pcgb_box* b) { return b->dfl ? (b->pairs ? kElemDDPair : kElemDD) : b->tb; }
 
 static void fill_physics(pcgb_box* b) {
   const pcgb_params& p = b->p;
@@ -215,9 +215,11 @@ static int upload_forcing(pcgb_box* b) {
 
 static int encode_maps(pcgb_box* b) {
   for (int q = 0; q < 2; ++q) {
-    cuuint64_t dims[4] = {(cuuint64_t)b->px, (cuuint64_t)b->my, (cuuint64_t)b->mz, (cuuint64_t)b->ns};
+    // a 16-byte double-float pair travels as two 8-byte TMA elements
+    const int sub = b->eb == 16 ? 2 : 1;
+    cuuint64_t dims[4] = {(cuuint64_t)b->px * sub, (cuuint64_t)b->my, (cuuint64_t)b->mz, (cuuint64_t)b->ns};
     cuuint64_t strides[3] = {(cuuint64_t)b->px * b->eb, (cuuint64_t)b->ps * b->eb, (cuuint64_t)b->fs * b->eb};
-    cuuint32_t box[4] = {(cuuint32_t)(b->tx + 8), (cuuint32_t)(b->ty + 6), 1u, (cuuint32_t)b->ns};
+    cuuint32_t box[4] = {(cuuint32_t)((b->tx + 8) * sub), (cuuint32_t)(b->ty + 6), 1u, (cuuint32_t)b->ns};
     cuuint32_t es[4] = {1, 1, 1, 1};
     // TMA moves bytes: a float2 pair travels as one 8-byte element
     CUresult r = g.encode(&b->hdev.tmap[q], b->eb == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
@@ -237,17 +239,18 @@ static int default_zdepth(const pcgb_box* b) {
   return zd;
 }
 
-// FP32: packed pairs on (32,8) tiles, one 8-warp CTA per SM; FP64 and
-// double-float: one 6-warp CTA per SM, (32,6) with 7 fields, (24,8) with 8
-// (an 8-field ring of (32,6) planes needs 246 KB of shared memory)
-static int default_tile(int tb, int nf) { return tb == 4 ? 5 : (nf == 8 ? 2 : 3); }
+// FP32: packed pairs on (32,8) tiles, one 8-warp CTA per SM; double-float:
+// packed pairs on (16,12) tiles, one 6-warp CTA per SM; FP64: one 6-warp CTA
+// per SM, (32,6) with 7 fields, (24,8) with 8 (an 8-field ring of (32,6)
+// planes needs 246 KB of shared memory)
+static int default_tile(int tb, int nf, int dfl) { return tb == 4 ? 5 : (dfl ? 5 : (nf == 8 ? 2 : 3)); }
 
 static int set_tiling(pcgb_box* b, int tile, int zd) {
-  if (tile < 0) tile = default_tile(b->tb, b->nf);
-  if (tile >= num_tiles(b->tb)) return set_err(PCGB_E_ARG, "tile variant %d out of range", tile);
-  if ((int)tile_is_pair(b->tb, tile) != b->pairs)
+  if (tile < 0) tile = default_tile(b->tb, b->nf, b->dfl);
+  if (tile >= num_tiles(b->tb, b->dfl)) return set_err(PCGB_E_ARG, "tile variant %d out of range", tile);
+  if ((int)tile_is_pair(b->tb, tile, b->dfl) != b->pairs)
     return set_err(PCGB_E_ARG, "tile %d needs a different device layout than this box was created with", tile);
-  TileShape ts = tile_shape(b->tb, tile);
+  TileShape ts = tile_shape(b->tb, tile, b->dfl);
   KernelHandle kh = get_kernel(b->tb, b->nf, tile, b->dfl);
   if (!kh.fn) return set_err(PCGB_E_ARG, "no kernel for tile %d", tile);
   if (kh.smem > g.max_smem) return set_err(PCGB_E_UNSUPPORTED, "tile %d needs %d B shared memory", tile, kh.smem);
@@ -306,10 +309,10 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   b->nx = p->nx; b->ny = p->ny; b->nz = p->nz;
   b->mx = p->nx + 6; b->my = p->ny + 6; b->mz = p->nz + 6;
   {
-    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb, b->nf);
-    b->pairs = (t0 < num_tiles(b->tb) && tile_is_pair(b->tb, t0)) ? 1 : 0;
+    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb, b->nf, b->dfl);
+    b->pairs = (t0 < num_tiles(b->tb, b->dfl) && tile_is_pair(b->tb, t0, b->dfl)) ? 1 : 0;
   }
-  b->eb = b->pairs ? 8 : b->tb;
+  b->eb = b->pairs ? (b->dfl ? 16 : 8) : b->tb;
   b->ns = b->pairs ? 4 : b->nf;
   b->xoff = 128 / b->eb;
   b->px = b->xoff + ((b->nx + 8 + b->xoff - 1) / b->xoff) * b->xoff;
@@ -356,9 +359,10 @@ extern "C" void pcgb_box_destroy(pcgb_box* b) {
 extern "C" size_t pcgb_params_bytes(const pcgb_params* p) {
   if (!p || p->nx < 1 || p->ny < 1 || p->nz < 1 || (p->precision != 4 && p->precision != 8)) return 0;
   const int tb = p->precision, nf = p->lentropy ? 8 : 7;
-  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb, nf);
-  const int pairs = (t0 < num_tiles(tb) && tile_is_pair(tb, t0)) ? 1 : 0;
-  const int eb = pairs ? 8 : tb, ns = pairs ? 4 : nf;
+  const int dfl = (tb == 8 && p->dfloat) ? 1 : 0;
+  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb, nf, dfl);
+  const int pairs = (t0 < num_tiles(tb, dfl) && tile_is_pair(tb, t0, dfl)) ? 1 : 0;
+  const int eb = pairs ? (dfl ? 16 : 8) : tb, ns = pairs ? 4 : nf;
   const int xoff = 128 / eb;
   const long long px = xoff + ((p->nx + 8 + xoff - 1) / xoff) * xoff;
   const long long fs = px * (p->ny + 6) * (p->nz + 6);
@@ -511,7 +515,10 @@ extern "C" int pcgb_box_init_field(pcgb_box* b, int field, int kind, double ampl
     else if (b->nf == 8 && field == 4) { slice = 3; lane = 1; }
     else { slice = field - iax; lane = 1; }
   }
-  char* base = static_cast<char*>(b->f[in]) + (size_t)slice * b->fs * b->eb + (size_t)lane * b->tb;
+  // lane offset in bytes: one value (field-major / FP32 pairs) or one float of the
+  // double-float pair's hi half (its lo half is 8 bytes further)
+  const size_t lane_bytes = (b->dfl && b->pairs) ? 4 : (size_t)b->tb;
+  char* base = static_cast<char*>(b->f[in]) + (size_t)slice * b->fs * b->eb + (size_t)lane * lane_bytes;
   const pcgb_params& p = b->p;
   const int comp = (field < 3) ? field : 0;   // ABC component of uu
   CK(launch_init_field(elem_code(b), base, kind, kind == 2 ? comp : 0, ampl, a, bb, c, k, seed, b->nx, b->ny, b->nz, b->px,
@@ -758,8 +765,8 @@ extern "C" int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, doubl
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0); cudaEventCreate(&e1);
   double best = 1e30; int bt = -1, bz = 0;
-  const int ntile = num_tiles(p->precision);
-  for (int fam = 0; fam < (p->precision == 4 ? 2 : 1); ++fam) {
+  const int ntile = num_tiles(p->precision, p->dfloat);
+  for (int fam = 0; fam < ((p->precision == 4 || p->dfloat) ? 2 : 1); ++fam) {
   q.tile = fam * kNumScalarTiles;
   pcgb_box* b = pcgb_box_create(&q);
   if (!b) { cudaEventDestroy(e0); cudaEventDestroy(e1); return g_err; }

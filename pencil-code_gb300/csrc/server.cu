@@ -210,7 +210,8 @@ extern "C" long long pcgb_server_submit(pcgb_server* s, const pcgb_params* p, in
   if (!s || !p || nsteps < 1) return -1;
   Req* r = new Req();
   r->p = *p;
-  if (r->p.tile < 0) r->p.tile = (r->p.precision == 4) ? 6 : 1;   // (16,8) tiles suit small boxes
+  // (16,8) tiles suit small boxes: packed pairs for FP32 and double-float, field-major for FP64
+  if (r->p.tile < 0) r->p.tile = (r->p.precision == 4 || r->p.dfloat) ? 6 : 1;
   if (r->p.zdepth <= 0) r->p.zdepth = 16;
   r->nsteps = nsteps;
   r->seed = seed;

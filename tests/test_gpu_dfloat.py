@@ -116,3 +116,50 @@ def test_dfloat_tiles_agree_and_track_native_fp64(pc, ic):
             assert np.all(rel_err(g, g64) <= 1e-13)
         else:
             assert np.array_equal(g, base), (tile, zd)
+
+
+@pytest.mark.parametrize("lentropy", [0, 1])
+def test_dfloat_pair_tiles_equal_field_major(pc, ic, lentropy):
+    """The packed double-float pair layout (tiles 4-7) computes lane by lane the
+    same operations as the field-major double-float tiles: same field bits."""
+    kw = dict(nx=40, ny=24, nz=20, lentropy=lentropy, gamma=5.0 / 3.0 if lentropy else 1.0, nu=5e-3, eta=5e-3,
+              chi=5e-3 if lentropy else 0.0, dt=2e-3, precision=8, dfloat=1, lforcing_cont=1, ampl_ff=0.02, kf=1.0,
+              diag_every=1)
+    p0 = pc.default_params(tile=0, **kw)
+    f0 = iso_state(pc, ic, p0, ampl=1e-2, seed=31)
+    if lentropy:
+        ic.gaussian_noise(f0, p0, ["lnrho", "ss"], 1e-3, 32)
+    base = pc.Box(p0)
+    base.load(f0)
+    base.steps(3)
+    g0, d0 = base.store(), base.diag_raw()
+    for tile in (4, 5, 6, 7):
+        box = pc.Box(pc.default_params(tile=tile, **kw))
+        assert box.info()["pairs"] == 1 and box.info()["tile"] == tile
+        box.load(f0)
+        box.steps(3)
+        assert np.array_equal(box.store(), g0), tile
+        # FP64 reductions over a different tile decomposition: same sums up to order
+        np.testing.assert_allclose(box.diag_raw(), d0, rtol=1e-12, atol=1e-24)
+
+
+def test_dfloat_pair_oracle_and_device_init(pc, ic, orc):
+    """Pair-tile double-float state against the FP64 oracle after 100 steps, and
+    the device initial condition writes the same state into both layouts."""
+    p = iso_params(pc, dfloat=1, tile=4)
+    f0 = iso_state(pc, ic, p)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(100)
+    ref, _, _ = run_oracle(orc, p, f0, 100)
+    assert np.all(rel_err(box.store(), ref) <= TOL64)
+    outs = []
+    for tile in (0, 4):
+        b = pc.Box(iso_params(pc, dfloat=1, tile=tile))
+        for k in range(7):
+            b.init_field(k, "zero")
+        b.init_field(0, "abc", ampl=0.1, abc=(1.0, 0.5, 0.25), k=1.0)
+        for k in (4, 5, 6):
+            b.init_field(k, "noise", ampl=1e-3, seed=40 + k)
+        outs.append(b.store())
+    assert np.array_equal(outs[0], outs[1])

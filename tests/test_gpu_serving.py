@@ -22,7 +22,7 @@ def _req(pc, n, prec, ent, seed, nu, k):
 def _alone(pc, ens, p, steps, seed):
     q = pc.default_params()
     q.update(**p.as_dict())
-    q.tile = 6 if q.precision == 4 else 1
+    q.tile = 6 if (q.precision == 4 or q.dfloat) else 1
     q.zdepth = 16
     b = pc.Box(q)
     ens.init_box(b, q, seed)
