@@ -288,6 +288,8 @@ def run_ours(args):
         line = {
             "metric": "Gcell-updates/s per RK substep", "value": value, "unit": "Gcell-updates/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            # the reference's own unit (run.f90:740): microseconds per grid point per RK step
+            "us_per_pt_step": 1e3 * (ms / args.steps) / (cells * ws),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if prec == 4 else ("f32x2 (double-float)" if args.dfloat else "f64"),
             "data": "synthetic (seeded on device)",
