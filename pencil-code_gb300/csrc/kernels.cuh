@@ -35,9 +35,11 @@ inline TileShape tile_shape(int dtype_bytes, int tile, int dfl = 0) {
 }
 
 struct KernelHandle {
-  const void* fn = nullptr;
+  const void* fn = nullptr;        // with CFL / diagnostic reductions
+  const void* fn_nored = nullptr;  // without (same shared memory and block)
   int smem = 0;
   int threads = 0;
+  const void* pick(bool red) const { return red ? fn : fn_nored; }
 };
 
 // Defined in kernels_<type>_<nf>.cu.
@@ -68,10 +70,13 @@ static KernelHandle make_dd_pair_handle() {
 template <class CELL, int TX, int TY, int R, int MB>
 static KernelHandle make_kernel_handle() {
   KernelHandle h;
-  h.fn = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB>);
+  h.fn = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, true>);
+  h.fn_nored = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, false>);
   h.smem = DriverCfg<CELL, TX, TY, R>::SMEM_BYTES;
   h.threads = TX * TY;
-  cudaFuncSetAttribute(&mhd_substep_kernel<CELL, TX, TY, R, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(&mhd_substep_kernel<CELL, TX, TY, R, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       h.smem);
+  cudaFuncSetAttribute(&mhd_substep_kernel<CELL, TX, TY, R, MB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        h.smem);
   return h;
 }

@@ -49,7 +49,11 @@ struct DriverCfg {
   static constexpr int SMEM_BYTES = RED_OFF + NWARP * PCGB_NSLOT * 8 + 64;
 };
 
-template <class CELL, int TX, int TY, int RING, int MINB>
+// RED = false: the variant for launches in which no box reduces (substeps 2
+// and 3, and substep 1 with a fixed dt and no diagnostics due): no per-thread
+// FP64 accumulators, no reduction code.  The host picks it; a box that
+// nevertheless finds a reduction due flags PCGB_ERR_NORED.
+template <class CELL, int TX, int TY, int RING, int MINB, bool RED>
 __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs args) {
   using C = DriverCfg<CELL, TX, TY, RING>;
   using T = typename CELL::T;
@@ -130,7 +134,12 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
     fl.dtb = T(dt * rk_beta(s));
     // compensated mode: df_stored = df + e / (dt*beta_{s+1}*alpha_{s+1})
     fl.cinv = (fl.comp && s < 2) ? T(1.0 / (dt * rk_beta(s + 1) * rk_alpha(s + 1))) : T(0);
-    const bool need_red = fl.want_cfl || fl.want_diag;
+    if (!RED) {
+      if ((fl.want_cfl || fl.want_diag) && threadIdx.x == 0) atomicOr(&S->err, PCGB_ERR_NORED);
+      fl.want_cfl = false;
+      fl.want_diag = false;
+    }
+    const bool need_red = RED && (fl.want_cfl || fl.want_diag);
 
     // plane j of this tile is ring plane gplane + j: slot (sbase + j) % RING and
     // fill phase ((sbase + j) / RING + pbase) & 1

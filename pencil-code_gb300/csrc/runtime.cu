@@ -148,6 +148,7 @@ struct pcgb_box {
   int tiles = 0;
   unsigned long long nsub = 0;  // host mirror of the device substep counter
   bool dt_known = false;
+  bool diag_pending = false;    // a diagnostics request not yet served by a substep-1 launch
   KernelHandle kh;
 };
 
@@ -389,7 +390,7 @@ static int cur_in(const pcgb_box* b) { return (int)(b->nsub & 1ull); }
 
 // Launch one substep (or CFL pass) over boxes[0..n) of one class.
 static int launch(const PcgbBoxDev* dboxes, int nboxes, int total_tiles, unsigned int* counter, int mode,
-                  const KernelHandle& kh, int grid) {
+                  const KernelHandle& kh, int grid, bool red) {
   LaunchArgs a;
   a.boxes = dboxes;
   a.nboxes = nboxes;
@@ -400,13 +401,25 @@ static int launch(const PcgbBoxDev* dboxes, int nboxes, int total_tiles, unsigne
   a.inject_wait_failure = g.inject_wait_failure;
   if (counter) CK(cudaMemsetAsync(counter, 0, sizeof(unsigned int), g.stream));
   void* args[] = {&a};
-  CK(cudaLaunchKernel(kh.fn, dim3(grid), dim3(kh.threads), args, (size_t)kh.smem, g.stream));
+  CK(cudaLaunchKernel(kh.pick(red || mode == MODE_CFL), dim3(grid), dim3(kh.threads), args, (size_t)kh.smem,
+                      g.stream));
   ++g.launches;
   return 0;
 }
 
+// Whether a launch of this box may reduce (CFL dt or diagnostics): the CFL
+// pass, or substep 1 with the lagged CFL dt, periodic diagnostics or a pending
+// request.  Every other launch runs the reduction-free kernel variant.
+static bool box_needs_red(const pcgb_box* b, int mode) {
+  if (mode == MODE_CFL) return true;
+  if (b->nsub % 3 != 0) return false;
+  return b->hdev.dt_mode == PCGB_DT_LAGGED || b->hdev.diag_every > 0 || b->diag_pending;
+}
+
 static int box_launch(pcgb_box* b, int mode) {
-  return launch(b->ddev, 1, b->tiles, nullptr, mode, b->kh, b->tiles);
+  const int rc = launch(b->ddev, 1, b->tiles, nullptr, mode, b->kh, b->tiles, box_needs_red(b, mode));
+  if (mode == MODE_SUBSTEP && b->nsub % 3 == 0) b->diag_pending = false;
+  return rc;
 }
 
 // First timestep when the CFL condition decides it (GpuCalcDt, gpu_astaroth.cc:546).
@@ -629,6 +642,7 @@ extern "C" int pcgb_box_set_dt(pcgb_box* b, double dt) {
 }
 
 static int box_request_diag(pcgb_box* b) {
+  b->diag_pending = true;
   int one = 1;
   CK(cudaMemcpyAsync(reinterpret_cast<char*>(b->dstate) + offsetof(PcgbBoxState, diag_request), &one, sizeof(int),
                      cudaMemcpyHostToDevice, g.stream));
@@ -647,6 +661,7 @@ struct pcgb_batch {
   int grid = 0;
   KernelHandle kh;
   bool any_current = false;
+  bool red0 = false;   // some box reduces on every substep 1 (lagged CFL dt or periodic diagnostics)
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;
 };
@@ -675,6 +690,7 @@ extern "C" pcgb_batch* pcgb_batch_create(pcgb_box** boxes, int n, int persistent
     h[i].tile0 = t0;
     t0 += h[i].tiles;
     if (B->boxes[i]->hdev.dt_mode == PCGB_DT_CURRENT) B->any_current = true;
+    if (B->boxes[i]->hdev.dt_mode == PCGB_DT_LAGGED || B->boxes[i]->hdev.diag_every > 0) B->red0 = true;
   }
   B->total_tiles = t0;
   B->kh = boxes[0]->kh;
@@ -701,12 +717,23 @@ extern "C" void pcgb_batch_destroy(pcgb_batch* B) {
   delete B;
 }
 
+static bool batch_diag_pending(const pcgb_batch* B) {
+  for (const auto* b : B->boxes)
+    if (b->diag_pending) return true;
+  return false;
+}
+
 static int batch_substep(pcgb_batch* B, int s) {
   int rc;
   unsigned int* ctr = B->persistent ? B->counter : nullptr;
-  if (s == 0 && B->any_current && (rc = launch(B->ddev, (int)B->boxes.size(), B->total_tiles, ctr, MODE_CFL, B->kh, B->grid)))
+  if (s == 0 && B->any_current &&
+      (rc = launch(B->ddev, (int)B->boxes.size(), B->total_tiles, ctr, MODE_CFL, B->kh, B->grid, true)))
     return rc;
-  return launch(B->ddev, (int)B->boxes.size(), B->total_tiles, ctr, MODE_SUBSTEP, B->kh, B->grid);
+  const bool red = (s == 0) && (B->red0 || batch_diag_pending(B));
+  rc = launch(B->ddev, (int)B->boxes.size(), B->total_tiles, ctr, MODE_SUBSTEP, B->kh, B->grid, red);
+  if (s == 0)
+    for (auto* b : B->boxes) b->diag_pending = false;
+  return rc;
 }
 
 extern "C" int pcgb_batch_steps(pcgb_batch* B, int nsteps, int use_graph, int graph_steps) {
@@ -716,7 +743,9 @@ extern "C" int pcgb_batch_steps(pcgb_batch* B, int nsteps, int use_graph, int gr
   for (auto* b : B->boxes)
     if ((rc = box_ensure_dt(b))) return rc;
   int done = 0;
-  if (use_graph && graph_steps > 0 && nsteps >= graph_steps) {
+  // a pending diagnostics request is served by direct launches (the captured
+  // graph's substep-1 launches reduce only when the batch always does)
+  if (use_graph && graph_steps > 0 && nsteps >= graph_steps && !batch_diag_pending(B)) {
     if (!B->gexec || B->gsteps != graph_steps) {
       if (B->gexec) { cudaGraphExecDestroy(B->gexec); B->gexec = nullptr; }
       cudaGraph_t graph;
