@@ -65,6 +65,10 @@ typedef struct pcgb_params {
   int dfloat;              /* precision 8 only: 1 = FP64-class state and arithmetic as double-float
                               pairs (hi + lo FP32, 48-bit significand) on the FP32 pipes instead of
                               native FP64, whose rate on this GPU is 1/64 of FP32's */
+  int lforcing_hel;        /* random helical forcing (&forcing_run_pars iforce='helical') added to uu
+                              after every step; wavevectors from pcgb_box_set_kvectors / pcgb_set_kvectors */
+  int seed_ff;             /* seed of the forcing's random stream (ran0, general.f90:867) */
+  double force_hel;        /* &forcing_run_pars force (amplitude of the helical forcing) */
 } pcgb_params;
 
 /* Defaults of the reference (cdata.f90:211,235,239; eos_idealgas.f90:47;
@@ -190,6 +194,8 @@ void tf_save_checkpoint_c_(const char* model_name, const char* checkpoint_dir);
 
 /* Timestep of the plug-in's box: the value Fortran's set_dt would receive
    (gpu_astaroth.cc:1618-1634 calls set_dt from C++; a C caller reads it). */
+/* k.dat for the plug-in's box (see pcgb_box_set_kvectors); call before initializeGPU. */
+int pcgb_set_kvectors(const double* kxyz, int nk, double kav);
 double pcgb_get_dt(void);
 double pcgb_get_time(void);
 /* Request device diagnostics (urms, brms, ...) on the next substep 1. */
@@ -226,6 +232,12 @@ int pcgb_box_sync(pcgb_box* b);
 int pcgb_box_diag(pcgb_box* b, double* out, int nout);
 int pcgb_box_time(pcgb_box* b, double* t, double* dt, long long* nsub);
 int pcgb_box_set_dt(pcgb_box* b, double dt);
+/* Wavevector list of the random helical forcing, the content of the reference's
+   k.dat (forcing.f90:888-900): kxyz = kkx[0..nk), kky[0..nk), kkz[0..nk); kav
+   the average |k| given there.  Required before stepping a box with
+   lforcing_hel; boxes with helical forcing step through the box API and the
+   plug-in set (a batch refuses them). */
+int pcgb_box_set_kvectors(pcgb_box* b, const double* kxyz, int nk, double kav);
 /* Device bytes held by the box. */
 size_t pcgb_box_bytes(const pcgb_box* b);
 /* Device bytes a box with these parameters would hold (admission control). */

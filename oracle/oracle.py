@@ -79,6 +79,9 @@ def lib():
         L.orc_ran0.restype = C.c_double
         L.orc_gaunoise_vect.argtypes = [P, C.c_double, dp, C.c_int, C.c_int, C.POINTER(C.c_int)]
         L.orc_grid.argtypes = [P, dpc, dpc, dpc]
+        L.orc_helical_coefs.argtypes = [P, C.c_double, dpc, dpc, dpc, C.c_int, C.c_double, C.POINTER(C.c_int),
+                                        C.POINTER(HelRec)]
+        L.orc_add_helical.argtypes = [P, dp, C.POINTER(HelRec), C.c_double]
         _lib = L
     return _lib
 
@@ -144,6 +147,35 @@ def time_step(p: OrcParams, f: np.ndarray, df: np.ndarray, t: float, dt: float, 
     lib().orc_time_step(C.byref(p), f, df, C.byref(tt), C.byref(dd), int(ldt),
                         dg.ctypes.data if dg is not None else None, nthreads)
     return tt.value, dd.value, dg
+
+
+class HelRec(C.Structure):
+    """orc_helrec: one time step's random helical forcing record."""
+    _fields_ = [("kk", C.c_double * 3), ("phase", C.c_double), ("coef1", C.c_double * 3),
+                ("coef2", C.c_double * 3), ("fact0", C.c_double)]
+
+
+def helical_coefs(p: OrcParams, force: float, kvec: np.ndarray, kav: float, state: int):
+    """fconst_coefs_hel with the ran0 stream: returns (record, new state); kvec is (3, nk)."""
+    kv = np.ascontiguousarray(kvec, dtype=np.float64)
+    s = C.c_int(state)
+    rec = HelRec()
+    lib().orc_helical_coefs(C.byref(p), force, kv[0], kv[1], kv[2], kv.shape[1], kav, C.byref(s), C.byref(rec))
+    return rec, s.value
+
+
+def add_helical(p: OrcParams, f: np.ndarray, rec: HelRec, dt: float) -> None:
+    """forcing_hel: f(uu) += the step's helical forcing (interior; refresh ghosts after)."""
+    lib().orc_add_helical(C.byref(p), f, C.byref(rec), dt)
+
+
+def read_kdat(path: str):
+    """k.dat of the reference (forcing.f90:888-900): 'nk kav', then kkx, kky, kkz."""
+    with open(path) as fh:
+        vals = fh.read().split()
+    nk, kav = int(vals[0]), float(vals[1])
+    k = np.array([float(v) for v in vals[2:2 + 3 * nk]]).reshape(3, nk)
+    return k, kav
 
 
 def gaunoise_vect(p: OrcParams, ampl: float, f: np.ndarray, i1: int, i2: int, state: int) -> int:

@@ -501,3 +501,71 @@ void orc_gaunoise_vect(const orc_params* p, double ampl, double* f, int i1, int 
       }
   free(r); free(q);
 }
+
+/* fconst_coefs_hel, forcing.f90:1763-1880 (default options: no shear, no
+   k-vector scaling, the new polarisation vectors, fda = 1, slope_ff = 0). */
+void orc_helical_coefs(const orc_params* p, double force, const double* kkx, const double* kky, const double* kkz,
+                       int nk, double kav, int* state, orc_helrec* rec) {
+  const double pi = 3.14159265358979323846264338327950;
+  const double fran1 = orc_ran0(state), fran2 = orc_ran0(state);
+  const double phase = pi * (2.0 * fran1 - 1.0);
+  const int ik = (int)((double)nk * (0.9999 * fran2) + 1.0);   /* 1-based */
+  const double kx = kkx[ik - 1], ky = kky[ik - 1], kz = kkz[ik - 1];
+  const double k2 = (kx * kx + ky * ky) + kz * kz;
+  const double k = sqrt(k2);
+  double ex, ey, ez;
+  if (ky == 0.0 && kz == 0.0) { ex = 0.0; ey = 1.0; ez = 0.0; } else { ex = 1.0; ey = 0.0; ez = 0.0; }
+  /* e1 = kk x ee, e2 = kk x e1, unit vectors (sub.f90 cross / dot2) */
+  double e1[3] = {ky * ez - kz * ey, kz * ex - kx * ez, kx * ey - ky * ex};
+  double norm = (e1[0] * e1[0] + e1[1] * e1[1]) + e1[2] * e1[2];
+  for (int i = 0; i < 3; ++i) e1[i] = e1[i] / sqrt(norm);
+  double e2[3] = {ky * e1[2] - kz * e1[1], kz * e1[0] - kx * e1[2], kx * e1[1] - ky * e1[0]};
+  norm = (e2[0] * e2[0] + e2[1] * e2[1]) + e2[2] * e2[2];
+  for (int i = 0; i < 3; ++i) e2[i] = e2[i] / sqrt(norm);
+  const double phi = orc_ran0(state) * 2.0 * pi;
+  ex = cos(phi) * e1[0] + sin(phi) * e2[0];
+  ey = cos(phi) * e1[1] + sin(phi) * e2[1];
+  ez = cos(phi) * e1[2] + sin(phi) * e2[2];
+  const double kde = (kx * ex + ky * ey) + kz * ez;
+  const double kex = ky * ez - kz * ey, key = kz * ex - kx * ez, kez = kx * ey - ky * ex;
+  const double kkex = ky * kez - kz * key, kkey = kz * kex - kx * kez, kkez = kx * key - ky * kex;
+  const double cs0eff = p->cs0;
+  const double ffnorm = sqrt(1.0 + p->relhel * p->relhel) * k * sqrt(k2 - kde * kde) / sqrt(kav * (cs0eff * cs0eff * cs0eff));
+  rec->kk[0] = kx; rec->kk[1] = ky; rec->kk[2] = kz;
+  rec->phase = phase;
+  rec->coef1[0] = k * kex; rec->coef1[1] = k * key; rec->coef1[2] = k * kez;
+  rec->coef2[0] = p->relhel * kkex; rec->coef2[1] = p->relhel * kkey; rec->coef2[2] = p->relhel * kkez;
+  rec->fact0 = force / ffnorm;
+}
+
+/* forcing_hel, forcing.f90:2066-2474, default path, with fxyz_coefs_hel
+   (:1882-1930): fx = exp(i(kx k1 x + phase)) fact, fy = exp(i ky k1 y),
+   fz = exp(i kz k1 z); f(uu_j) += Re[(coef1_j + i coef2_j) (fx fy) fz]. */
+void orc_add_helical(const orc_params* p, double* f, const orc_helrec* rec, double dt) {
+  const int mx = p->nx + 2 * NG, my = p->ny + 2 * NG, mz = p->nz + 2 * NG;
+  const double fact = rec->fact0 * sqrt(dt);
+  const double k1 = p->kf;
+  double* x = malloc(sizeof(double) * (mx + my + mz));
+  double* y = x + mx;
+  double* z = y + my;
+  orc_grid(p, x, y, z);
+  for (int n = NG; n < NG + p->nz; ++n) {
+    const double az = rec->kk[2] * k1 * z[n];
+    const double fzr = cos(az), fzi = sin(az);
+    for (int m = NG; m < NG + p->ny; ++m) {
+      const double ay = rec->kk[1] * k1 * y[m];
+      const double fyr = cos(ay), fyi = sin(ay);
+      for (int l = NG; l < NG + p->nx; ++l) {
+        const double ax = rec->kk[0] * k1 * x[l] + rec->phase;
+        const double fxr = cos(ax) * fact, fxi = sin(ax) * fact;
+        const double pr = fxr * fyr - fxi * fyi, pim = fxr * fyi + fxi * fyr;   /* fx fy */
+        const double qr = pr * fzr - pim * fzi, qi = pr * fzi + pim * fzr;      /* (fx fy) fz */
+        for (int j = 0; j < 3; ++j) {
+          const size_t o = (size_t)l + (size_t)mx * ((size_t)m + (size_t)my * ((size_t)n + (size_t)mz * j));
+          f[o] = f[o] + (rec->coef1[j] * qr - rec->coef2[j] * qi);
+        }
+      }
+    }
+  }
+  free(x);
+}

@@ -69,6 +69,22 @@ void orc_pde(const orc_params* p, const double* f, double* df, double alpha,
 void orc_time_step(const orc_params* p, double* f, double* df, double* t, double* dt,
                    int ldt, double* diag, int nthreads);
 
+/* Random helical forcing (iforce='helical'), default path: one record per
+   time step from fconst_coefs_hel (src/forcing.f90:1763-1880) -- wavevector
+   k drawn from the k.dat list, phase and polarisation angle from the random
+   stream (two draws fran(1:2), then phi, as the reference draws them; here the
+   stream is ran0) -- then forcing_hel (:2066-2474) with fxyz_coefs_hel
+   (:1882-1930) adds Re[(coef1 + i coef2) fx fy fz] to uu after the step
+   (addforce, :1307), fact = force/ffnorm*sqrt(dt).  k1_ff is p->kf, cs0eff
+   is p->cs0 (initialize_forcing, :1075-1082), slope_ff = 0. */
+typedef struct {
+  double kk[3], phase, coef1[3], coef2[3], fact0;   /* fact0 = force/ffnorm (times sqrt(dt) on use) */
+} orc_helrec;
+void orc_helical_coefs(const orc_params* p, double force, const double* kkx, const double* kky, const double* kkz,
+                       int nk, double kav, int* state, orc_helrec* rec);
+/* f(uu) += forcing over the interior (ghosts are the caller's to refresh). */
+void orc_add_helical(const orc_params* p, double* f, const orc_helrec* rec, double dt);
+
 /* The reference 'min_std' generator ran0 (src/general.f90:867-889) and
    gaunoise_vect (src/initcond.f90:5005-5047). */
 double orc_ran0(int* state);

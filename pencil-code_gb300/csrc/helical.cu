@@ -1,0 +1,183 @@
+// helical.cu -- random helical forcing, iforce='helical' (forcing.f90:1307
+// addforce, :2066-2474 forcing_hel, :1763-1880 fconst_coefs_hel, :1882-1930
+// fxyz_coefs_hel), default options: no shear, no k-vector scaling, the new
+// polarisation vectors, fda = 1, unit profiles, slope_ff = 0, cs0eff = cs0.
+//
+// After every time step the force, a single helical Fourier mode of the
+// wavevector list, is added to uu as an Euler step (constant over the step):
+//   uu_j += Re[(coef1_j + i coef2_j) fx(x) fy(y) fz(z)],
+//   fx = exp(i(kx k1 x + phase)) force/ffnorm sqrt(dt), fy = exp(i ky k1 y),
+//   fz = exp(i kz k1 z).
+// The host draws each step's wavevector, phase and polarisation angle; a
+// one-block kernel builds the 1-D factor tables of the completed step on the
+// device (dt is the device's), and a second kernel applies them to every
+// interior cell and its periodic ghost images.
+#include <cmath>
+
+#include "dd.cuh"
+#include "helical.h"
+#include "mhd_common.cuh"
+
+namespace pcgb {
+
+// ran0 (general.f90:867-889): Lewis-Goodman-Miller minimal standard
+// generator with the reference's XOR mask.
+static double ran0(int* state) {
+  const int ia = 16807, im = 2147483647, iq = 127773, ir = 2836, mask = 123459876;
+  *state = *state ^ mask;
+  const int k = *state / iq;
+  *state = ia * (*state - k * iq) - ir * k;
+  if (*state < 0) *state = *state + im;
+  const double r = (1.0 / (double)im) * (double)(*state);
+  *state = *state ^ mask;
+  return r;
+}
+
+void helical_record(double cs0, double relhel, double force, const double* kxyz, int nk, double kav, int* state,
+                    HelRec* rec) {
+  const double pi = 3.14159265358979323846264338327950;
+  const double fran1 = ran0(state), fran2 = ran0(state);
+  const double phase = pi * (2.0 * fran1 - 1.0);
+  const int ik = (int)((double)nk * (0.9999 * fran2) + 1.0);   // 1-based, forcing.f90:1798
+  const double kx = kxyz[ik - 1], ky = kxyz[nk + ik - 1], kz = kxyz[2 * nk + ik - 1];
+  const double k2 = (kx * kx + ky * ky) + kz * kz;
+  const double k = std::sqrt(k2);
+  double ex = 1.0, ey = 0.0, ez = 0.0;
+  if (ky == 0.0 && kz == 0.0) { ex = 0.0; ey = 1.0; }
+  // unit vectors perpendicular to k: e1 = k x e, e2 = k x e1 (forcing.f90:1858-1866)
+  double e1[3] = {ky * ez - kz * ey, kz * ex - kx * ez, kx * ey - ky * ex};
+  double nrm = (e1[0] * e1[0] + e1[1] * e1[1]) + e1[2] * e1[2];
+  for (double& v : e1) v = v / std::sqrt(nrm);
+  double e2[3] = {ky * e1[2] - kz * e1[1], kz * e1[0] - kx * e1[2], kx * e1[1] - ky * e1[0]};
+  nrm = (e2[0] * e2[0] + e2[1] * e2[1]) + e2[2] * e2[2];
+  for (double& v : e2) v = v / std::sqrt(nrm);
+  const double phi = ran0(state) * 2.0 * pi;
+  ex = std::cos(phi) * e1[0] + std::sin(phi) * e2[0];
+  ey = std::cos(phi) * e1[1] + std::sin(phi) * e2[1];
+  ez = std::cos(phi) * e1[2] + std::sin(phi) * e2[2];
+  const double kde = (kx * ex + ky * ey) + kz * ez;
+  const double kex = ky * ez - kz * ey, key = kz * ex - kx * ez, kez = kx * ey - ky * ex;
+  const double kkex = ky * kez - kz * key, kkey = kz * kex - kx * kez, kkez = kx * key - ky * kex;
+  const double ffnorm = std::sqrt(1.0 + relhel * relhel) * k * std::sqrt(k2 - kde * kde) / std::sqrt(kav * (cs0 * cs0 * cs0));
+  rec->kk[0] = kx; rec->kk[1] = ky; rec->kk[2] = kz;
+  rec->phase = phase;
+  rec->coef1[0] = k * kex; rec->coef1[1] = k * key; rec->coef1[2] = k * kez;
+  rec->coef2[0] = relhel * kkex; rec->coef2[1] = relhel * kkey; rec->coef2[2] = relhel * kkez;
+  rec->fact0 = force / ffnorm;
+}
+
+// tab: coef1[3], coef2[3], 2 spare, then fx, fy, fz as (re, im) pairs.
+__global__ void helical_tables_kernel(const HelRec* ring, const PcgbBoxState* S, double* tab, HelGeom g) {
+  const unsigned long long step = S->nsub / 3ull - 1ull;   // the step just completed
+  const HelRec r = ring[step % (unsigned long long)kHelRing];
+  const double fact = __dmul_rn(r.fact0, sqrt(S->dt_last));
+  if (threadIdx.x < 3) {
+    tab[threadIdx.x] = r.coef1[threadIdx.x];
+    tab[3 + threadIdx.x] = r.coef2[threadIdx.x];
+  }
+  double* fx = tab + 8;
+  double* fy = fx + 2 * g.nx;
+  double* fz = fy + 2 * g.ny;
+  for (int i = threadIdx.x; i < g.nx + g.ny + g.nz; i += blockDim.x) {
+    if (i < g.nx) {
+      const double x = __dadd_rn(g.x0, __dmul_rn((double)i + 0.5, g.dx));
+      const double a = __dadd_rn(__dmul_rn(__dmul_rn(r.kk[0], g.k1), x), r.phase);
+      fx[2 * i] = __dmul_rn(cos(a), fact);
+      fx[2 * i + 1] = __dmul_rn(sin(a), fact);
+    } else if (i < g.nx + g.ny) {
+      const int j = i - g.nx;
+      const double y = __dadd_rn(g.y0, __dmul_rn((double)j + 0.5, g.dy));
+      const double a = __dmul_rn(__dmul_rn(r.kk[1], g.k1), y);
+      fy[2 * j] = cos(a);
+      fy[2 * j + 1] = sin(a);
+    } else {
+      const int k = i - g.nx - g.ny;
+      const double z = __dadd_rn(g.z0, __dmul_rn((double)k + 0.5, g.dz));
+      const double a = __dmul_rn(__dmul_rn(r.kk[2], g.k1), z);
+      fz[2 * k] = cos(a);
+      fz[2 * k + 1] = sin(a);
+    }
+  }
+}
+
+// arithmetic without contraction, in the precision of the state
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+
+// uu_j element e (units of the layout's element) += v
+template <int LAYOUT, typename R>
+__device__ __forceinline__ void add_u(void* f, long long e, R v) {
+  if (LAYOUT == HEL_F32) {
+    float* p = static_cast<float*>(f) + e;
+    *p = radd(*p, (float)v);
+  } else if (LAYOUT == HEL_F64) {
+    double* p = static_cast<double*>(f) + e;
+    *p = radd(*p, (double)v);
+  } else if (LAYOUT == HEL_F32_PAIR) {
+    float* p = static_cast<float*>(f) + 2 * e;   // lane 0 of the (u, A) pair
+    *p = radd(*p, (float)v);
+  } else {
+    float* p = static_cast<float*>(f) + (LAYOUT == HEL_DD ? 2 * e : 4 * e);
+    const int lo = (LAYOUT == HEL_DD) ? 1 : 2;   // dd: (hi, lo); dd2 lane 0: hi at 0, lo at 2
+    const dd w(__dadd_rn((double)p[0] + (double)p[lo], (double)v));
+    p[0] = w.hi;
+    p[lo] = w.lo;
+  }
+}
+
+template <int LAYOUT, typename R>
+__global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
+  const double* fx = tab + 8;
+  const double* fy = fx + 2 * g.nx;
+  const double* fz = fy + 2 * g.ny;
+  R c1[3], c2[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) { c1[j] = (R)tab[j]; c2[j] = (R)tab[3 + j]; }
+  const long long total = (long long)g.nx * g.ny * g.nz;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q % g.nx);
+    const long long rr = q / g.nx;
+    const int j = (int)(rr % g.ny);
+    const int k = (int)(rr / g.ny);
+    const R xr = (R)fx[2 * i], xi = (R)fx[2 * i + 1];
+    const R yr = (R)fy[2 * j], yi = (R)fy[2 * j + 1];
+    const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
+    const R pr = rsub(rmul(xr, yr), rmul(xi, yi)), pi = radd(rmul(xr, yi), rmul(xi, yr));   // fx fy
+    const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
+    R fc[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fc[c] = rsub(rmul(c1[c], qr), rmul(c2[c], qi));
+    const Images ix(i, g.nx), iy(j, g.ny), iz(k, g.nz);
+    for (int a = 0; a < iz.n; ++a)
+      for (int b = 0; b < iy.n; ++b)
+        for (int e = 0; e < ix.n; ++e) {
+          const long long cell = (long long)(iz.v[a] + 3) * g.ps + (long long)(iy.v[b] + 3) * g.px + g.xoff + ix.v[e];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) add_u<LAYOUT, R>(f, c * g.fs + cell, fc[c]);
+        }
+  }
+}
+
+cudaError_t launch_helical(int layout, void* f, const HelRec* ring, const PcgbBoxState* state, double* tab,
+                           const HelGeom& g, cudaStream_t s) {
+  helical_tables_kernel<<<1, 256, 0, s>>>(ring, state, tab, g);
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 65535LL * 16) blocks = 65535LL * 16;
+  const int gb = (int)(blocks < 1 ? 1 : blocks);
+  switch (layout) {
+    case HEL_F32: helical_apply_kernel<HEL_F32, float><<<gb, 256, 0, s>>>(f, tab, g); break;
+    case HEL_F64: helical_apply_kernel<HEL_F64, double><<<gb, 256, 0, s>>>(f, tab, g); break;
+    case HEL_DD: helical_apply_kernel<HEL_DD, double><<<gb, 256, 0, s>>>(f, tab, g); break;
+    case HEL_F32_PAIR: helical_apply_kernel<HEL_F32_PAIR, float><<<gb, 256, 0, s>>>(f, tab, g); break;
+    default: helical_apply_kernel<HEL_DD_PAIR, double><<<gb, 256, 0, s>>>(f, tab, g); break;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace pcgb

@@ -1,0 +1,38 @@
+// helical.h -- random helical forcing (iforce='helical') added to uu after a time step.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pcgb_box.h"
+
+namespace pcgb {
+
+// One time step's forcing, fconst_coefs_hel (forcing.f90:1763-1880):
+// wavevector, phase, the two polarisation coefficient vectors and
+// force/ffnorm (the device multiplies by sqrt(dt) of the step).
+struct HelRec {
+  double kk[3], phase, coef1[3], coef2[3], fact0;
+};
+
+constexpr int kHelRing = 64;   // records kept on the device, indexed by step % kHelRing
+
+// Draw the record of the next step from the ran0 stream `state` (two draws for
+// phase and wavevector, one for the polarisation angle, as the reference draws them).
+void helical_record(double cs0, double relhel, double force, const double* kxyz, int nk, double kav, int* state,
+                    HelRec* rec);
+
+// Element layout of the box's f array.
+enum HelLayout { HEL_F32 = 0, HEL_F64 = 1, HEL_DD = 2, HEL_F32_PAIR = 3, HEL_DD_PAIR = 4 };
+
+struct HelGeom {
+  int nx, ny, nz, px, my, xoff;
+  long long ps, fs;   // plane and slice strides in elements
+  double x0, y0, z0, dx, dy, dz, k1;
+};
+
+// Tables of the completed step (record ring[(nsub/3 - 1) % kHelRing], dt_last
+// of `state`) into `tab`, then uu += Re[(coef1 + i coef2) fx fy fz] on every
+// interior cell and its periodic ghost images.
+cudaError_t launch_helical(int layout, void* f, const HelRec* ring, const PcgbBoxState* state, double* tab,
+                           const HelGeom& g, cudaStream_t s);
+
+}  // namespace pcgb

@@ -307,6 +307,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
           ds = ds + 1.0;
           S->ds = ds;
           S->t = S->t + ds * (dt * rk_beta(s));
+          if (s == 2) S->dt_last = dt;
           if (s == 2 && bdt_mode == PCGB_DT_LAGGED) S->dt = S->dt_next;
           S->nsub = nsub + 1ull;
         }

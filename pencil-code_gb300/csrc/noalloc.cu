@@ -66,6 +66,7 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
     return fail(2, "invalid argument");
   if (p->precision != 4 && p->precision != 8) return fail(2, "precision must be 4 or 8");
   if (p->dfloat) return fail(2, "double-float state is not available here (use the box API)");
+  if (p->lforcing_hel) return fail(2, "the step-end helical forcing is applied by the box API only");
   if (p->nx < 6 || p->ny < 6 || p->nz < 6 || p->nx > kMaxExtent || p->ny > kMaxExtent || p->nz > kMaxExtent)
     return fail(7, "grid extent outside [6, PCGB_NOALLOC_MAX_EXTENT]");
   cudaStream_t s = static_cast<cudaStream_t>(stream);

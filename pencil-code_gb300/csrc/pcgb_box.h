@@ -75,6 +75,7 @@ struct alignas(64) PcgbBoxState {
   double diag[PCGB_NSLOT];   // last reduced diagnostics (sums and maxima)
   int diag_request;          // host request: diagnostics at the next substep 1
   int pad_[3];
+  double dt_last;            // dt of the last completed step (the step-end helical forcing scales with it)
 };
 
 #define PCGB_ERR_NONFINITE 1   // NaN/Inf seen in dt1

@@ -26,6 +26,7 @@
 
 #include "../../include/pcgb300.h"
 #include "aux_kernels.h"
+#include "helical.h"
 #include "kernels.cuh"
 #include "pcgb_box.h"
 
@@ -150,6 +151,13 @@ struct pcgb_box {
   bool dt_known = false;
   bool diag_pending = false;    // a diagnostics request not yet served by a substep-1 launch
   KernelHandle kh;
+  // random helical forcing: wavevector list (kkx, kky, kkz), its mean |k|, the
+  // ran0 stream, the device record ring and factor tables
+  std::vector<double> kvec;
+  double kav = 0.0;
+  int rng = 0;
+  HelRec* dring = nullptr;
+  double* dtab = nullptr;
 };
 
 // Element code of the layout kernels: float, double or double-float.
@@ -278,7 +286,7 @@ static int set_tiling(pcgb_box* b, int tile, int zd) {
 static void box_free(pcgb_box* b) {
   if (!b) return;
   cudaFree(b->f[0]); cudaFree(b->f[1]); cudaFree(b->df); cudaFree(b->forc); cudaFree(b->partial);
-  cudaFree(b->dstate); cudaFree(b->ddev);
+  cudaFree(b->dstate); cudaFree(b->ddev); cudaFree(b->dring); cudaFree(b->dtab);
   delete b;
 }
 
@@ -296,6 +304,8 @@ static int validate(const pcgb_params* p) {
     return set_err(PCGB_E_ARG, "cs0, rho0, cp, gamma, mu0 must be positive");
   if (!(p->cdt > 0 && p->cdtv > 0)) return set_err(PCGB_E_ARG, "cdt and cdtv must be positive");
   if (p->dt < 0) return set_err(PCGB_E_ARG, "dt must be >= 0");
+  if (p->lforcing_hel != 0 && p->lforcing_hel != 1) return set_err(PCGB_E_ARG, "lforcing_hel must be 0 or 1");
+  if (p->lforcing_hel && !(p->force_hel >= 0.0)) return set_err(PCGB_E_ARG, "force_hel must be >= 0");
   return 0;
 }
 
@@ -333,6 +343,10 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   if (cudaMalloc(&b->forc, nforc * b->tb) != cudaSuccess) return fail("forcing tables");
   if (cudaMalloc(&b->dstate, sizeof(PcgbBoxState)) != cudaSuccess) return fail("state");
   if (cudaMalloc(&b->ddev, sizeof(PcgbBoxDev)) != cudaSuccess) return fail("descriptor");
+  if (cudaMalloc(&b->dring, sizeof(HelRec) * kHelRing) != cudaSuccess ||
+      cudaMalloc(&b->dtab, sizeof(double) * (8 + 2 * ((size_t)b->nx + b->ny + b->nz))) != cudaSuccess)
+    return fail("helical forcing tables");
+  b->rng = p->seed_ff;
   cudaMemsetAsync(b->f[0], 0, b->fbytes, g.stream);
   cudaMemsetAsync(b->f[1], 0, b->fbytes, g.stream);
   cudaMemsetAsync(b->df, 0, b->fbytes, g.stream);
@@ -578,15 +592,61 @@ extern "C" int pcgb_box_store(pcgb_box* b, double* fh) {
   return box_check_state(b);
 }
 
+// Layout code of the helical forcing kernels.
+static int hel_layout(const pcgb_box* b) {
+  if (b->tb == 4) return b->pairs ? HEL_F32_PAIR : HEL_F32;
+  if (b->dfl) return b->pairs ? HEL_DD_PAIR : HEL_DD;
+  return HEL_F64;
+}
+
+// Random helical forcing of the step that starts now: draw its record into the
+// device ring (forcing.f90 fconst_coefs_hel), applied when the step ends.
+static int helical_begin_step(pcgb_box* b) {
+  if (b->kvec.empty()) return set_err(PCGB_E_STATE, "helical forcing needs wavevectors (pcgb_box_set_kvectors)");
+  HelRec rec;
+  const int nk = (int)(b->kvec.size() / 3);
+  helical_record(b->p.cs0, b->p.relhel, b->p.force_hel, b->kvec.data(), nk, b->kav, &b->rng, &rec);
+  CK(cudaMemcpyAsync(b->dring + (b->nsub / 3) % kHelRing, &rec, sizeof(rec), cudaMemcpyHostToDevice, g.stream));
+  return 0;
+}
+
+// addforce (forcing.f90:1307) after the step: uu of the new state += the force.
+static int helical_end_step(pcgb_box* b) {
+  const pcgb_params& p = b->p;
+  HelGeom hg;
+  hg.nx = b->nx; hg.ny = b->ny; hg.nz = b->nz; hg.px = b->px; hg.my = b->my; hg.xoff = b->xoff;
+  hg.ps = b->ps; hg.fs = b->fs;
+  hg.x0 = p.xyz0[0]; hg.y0 = p.xyz0[1]; hg.z0 = p.xyz0[2];
+  hg.dx = p.Lxyz[0] / p.nx; hg.dy = p.Lxyz[1] / p.ny; hg.dz = p.Lxyz[2] / p.nz;
+  hg.k1 = p.kf;
+  CK(launch_helical(hel_layout(b), b->f[cur_in(b)], b->dring, b->dstate, b->dtab, hg, g.stream));
+  g.launches += 2;
+  return 0;
+}
+
 static int box_substep(pcgb_box* b) {
   const int s = (int)(b->nsub % 3);
   int rc;
   if (s == 0) {
     if ((rc = box_ensure_dt(b))) return rc;
     if (b->hdev.dt_mode == PCGB_DT_CURRENT && (rc = box_launch(b, MODE_CFL))) return rc;
+    if (b->p.lforcing_hel && (rc = helical_begin_step(b))) return rc;
   }
   if ((rc = box_launch(b, MODE_SUBSTEP))) return rc;
   b->nsub++;
+  if (s == 2 && b->p.lforcing_hel && (rc = helical_end_step(b))) return rc;
+  return 0;
+}
+
+extern "C" int pcgb_box_set_kvectors(pcgb_box* b, const double* kxyz, int nk, double kav) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!b || !kxyz || nk < 1 || !(kav > 0.0)) return set_err(PCGB_E_ARG, "bad wavevector list");
+  for (int i = 0; i < nk; ++i) {
+    const double kx = kxyz[i], ky = kxyz[nk + i], kz = kxyz[2 * nk + i];
+    if (kx * kx + ky * ky + kz * kz == 0.0) return set_err(PCGB_E_ARG, "wavevector %d is zero", i);
+  }
+  b->kvec.assign(kxyz, kxyz + 3 * (size_t)nk);
+  b->kav = kav;
   return 0;
 }
 
@@ -679,6 +739,11 @@ extern "C" pcgb_batch* pcgb_batch_create(pcgb_box** boxes, int n, int persistent
       return nullptr;
     }
     if (b->nsub % 3 != 0) { set_err(PCGB_E_STATE, "box in the middle of a step"); delete B; return nullptr; }
+    if (b->p.lforcing_hel) {
+      set_err(PCGB_E_UNSUPPORTED, "random helical forcing steps through the box API, not in a batch");
+      delete B;
+      return nullptr;
+    }
   }
   std::stable_sort(B->boxes.begin(), B->boxes.end(), [](const pcgb_box* a, const pcgb_box* c) {
     return (long long)a->nx * a->ny * a->nz > (long long)c->nx * c->ny * c->nz;
@@ -850,6 +915,7 @@ extern "C" void pcgb_default_params(pcgb_params* p) {
   p->cdt = 0.9; p->cdtv = 0.25;
   p->dt = 0.0; p->dt_mode = PCGB_DT_LAGGED; p->diag_every = 0;
   p->tile = -1; p->zdepth = 0;
+  p->lforcing_hel = 0; p->force_hel = 0.0; p->seed_ff = 1812;   // seed0, cdata.f90:743
 }
 
 extern "C" int pcgb_last_error(void) { return g_err; }
@@ -889,6 +955,8 @@ extern "C" const char* pcgb_version(void) { return "pcgb300 1.0 sm_103a"; }
 static pcgb_params g_par;
 static bool g_par_set = false;
 static pcgb_box* g_box = nullptr;
+static std::vector<double> g_kvec;   // k.dat of the plug-in's box
+static double g_kav = 0.0;
 static double* g_hostf = nullptr;
 
 extern "C" int pcgb_set_params(const pcgb_params* p) {
@@ -912,6 +980,7 @@ extern "C" void initializeGPU(REAL_PCGB* f, int comm, double t, int nt, int read
   }
   g_box = pcgb_box_create(&p);
   if (!g_box) return;
+  if (!g_kvec.empty()) pcgb_box_set_kvectors(g_box, g_kvec.data(), (int)(g_kvec.size() / 3), g_kav);
   g_hostf = f;
   if (f && nt > 0) pcgb_box_load(g_box, f, t);   // gpu_astaroth.f90:236 load_farray_to_GPU
   else if (g_box) {
@@ -1103,6 +1172,14 @@ extern "C" void tf_create_model_c_api(const char*, const char*, int, bool) {}
 extern "C" void tf_train_c_api(const char*, REAL_PCGB*, int, double) {}
 extern "C" void tf_infer_c_api(const char*, int) {}
 extern "C" void print_debug(void) {}
+
+extern "C" int pcgb_set_kvectors(const double* kxyz, int nk, double kav) {
+  if (!kxyz || nk < 1 || !(kav > 0.0)) return set_err(PCGB_E_ARG, "bad wavevector list");
+  g_kvec.assign(kxyz, kxyz + 3 * (size_t)nk);
+  g_kav = kav;
+  if (g_box) return pcgb_box_set_kvectors(g_box, kxyz, nk, kav);
+  return 0;
+}
 
 extern "C" double pcgb_get_dt(void) {
   double dt = 0;

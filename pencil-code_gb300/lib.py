@@ -36,6 +36,7 @@ class Params(C.Structure):
         ("cdt", C.c_double), ("cdtv", C.c_double),
         ("dt", C.c_double), ("dt_mode", C.c_int), ("diag_every", C.c_int),
         ("tile", C.c_int), ("zdepth", C.c_int), ("dfloat", C.c_int),
+        ("lforcing_hel", C.c_int), ("seed_ff", C.c_int), ("force_hel", C.c_double),
     ]
 
     def update(self, **kw) -> "Params":
@@ -76,6 +77,7 @@ EXPORTS = [
     "radtransfer_gpu_c_", "get_gpu_reduced_vars_c_", "test_bcs_c_", "split_update_gpu_c_",
     "tf_train_c_", "tf_infer_c_", "tf_create_model_c_", "print_snapshot_c_", "tf_load_model_c_",
     "tf_load_model_checkpoint_c_", "tf_save_model_c_", "tf_save_checkpoint_c_",
+    "pcgb_box_set_kvectors", "pcgb_set_kvectors",
     "pcgb_get_dt", "pcgb_get_time", "pcgb_request_diagnostics", "pcgb_time_step",
     "pcgb_box_create", "pcgb_box_destroy", "pcgb_box_load", "pcgb_box_store", "pcgb_box_init_field", "pcgb_box_steps",
     "pcgb_box_sync", "pcgb_box_diag", "pcgb_box_time", "pcgb_box_set_dt", "pcgb_box_bytes",
@@ -142,6 +144,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "pcgb_box_diag": (C.c_int, [vp, dptr, C.c_int]),
         "pcgb_box_time": (C.c_int, [vp, dptr, dptr, C.POINTER(C.c_longlong)]),
         "pcgb_box_set_dt": (C.c_int, [vp, C.c_double]),
+        "pcgb_box_set_kvectors": (C.c_int, [vp, dptr, C.c_int, C.c_double]),
+        "pcgb_set_kvectors": (C.c_int, [dptr, C.c_int, C.c_double]),
         "pcgb_box_bytes": (C.c_size_t, [vp]),
         "pcgb_box_info": (C.c_int, [vp, C.POINTER(C.c_int), C.c_int]),
         "pcgb_batch_create": (vp, [C.POINTER(vp), C.c_int, C.c_int]),
@@ -174,16 +178,21 @@ class PcgbError(RuntimeError):
 
 
 def check(rc: int) -> None:
+    """Raise for a failed call; the sticky library error is cleared once raised."""
     if rc:
         L = load()
         msg = L.pcgb_error_string(rc).decode()
+        L.pcgb_clear_error()
         raise PcgbError(f"pcgb error {rc}: {msg}")
 
 
 def last_error() -> tuple[int, str]:
+    """The sticky library error (code, message), cleared by reading it."""
     L = load()
     rc = L.pcgb_last_error()
-    return rc, L.pcgb_error_string(rc).decode()
+    msg = L.pcgb_error_string(rc).decode()
+    L.pcgb_clear_error()
+    return rc, msg
 
 
 def default_params(**kw) -> Params:
@@ -265,6 +274,11 @@ class Box:
 
     def set_dt(self, dt: float):
         check(load().pcgb_box_set_dt(self.h, dt))
+
+    def set_kvectors(self, kvec: np.ndarray, kav: float):
+        """Helical forcing wavevectors, (3, nk) as in the reference's k.dat."""
+        kv = np.ascontiguousarray(kvec, dtype=np.float64)
+        check(load().pcgb_box_set_kvectors(self.h, _dptr(kv), kv.shape[1], kav))
 
     def nbytes(self) -> int:
         return int(load().pcgb_box_bytes(self.h))

@@ -17,6 +17,9 @@ nowhere else):
    with samples/1d-tests/axionSU2back_lhubble2 (data/proc0), copied as bytes,
    and what the reference's own Fortran record reader
    (python/pencil/read/fortran_file.py, FortranFileExt) reads from it.
+5. helical_mhdturb_ref.json -- samples/helical-MHDturb: the wavevector list
+   k.dat (random helical forcing) and the it / t / dt / umax / urms columns of
+   reference.out, with the sample's run parameters.
 4. var_subrecords.json -- a small snapshot written by
    pencil-code_gb300/vardat.py with a tiny subrecord size, checked at
    generation time to read back identically through FortranFileExt.
@@ -142,6 +145,26 @@ def main(ref_root):
         size = len(fh.read())
     os.remove(tmp)
     assert np.array_equal(f2, f) and g2[0] == 1.25
+    # helical forcing sample (k.dat and the regression series, read as text)
+    hdir = os.path.join(ref_root, "samples", "helical-MHDturb")
+    with open(os.path.join(hdir, "k.dat")) as fh:
+        vals = fh.read().split()
+    nk, kav = int(vals[0]), float(vals[1])
+    kk = [float(v) for v in vals[2:2 + 3 * nk]]
+    series = []
+    with open(os.path.join(hdir, "reference.out")) as fh:
+        for line in fh:
+            if line.startswith("#") or not line.strip():
+                continue
+            v = line.split()
+            series.append({"it": int(v[0]), "t": float(v[1]), "dt": float(v[2]), "umax": float(v[3]),
+                           "urms": float(v[4])})
+    hpar = {"n": 32, "gamma": 1.0, "nu": 5e-3, "eta": 5e-3, "iforce": "helical", "force": 0.07, "relhel": 1.0,
+            "dt": 4e-2, "nt": 10, "it1": 2, "cdt": 0.4, "cdtv": 0.3,
+            "source": "samples/helical-MHDturb/{start.in,run.in,k.dat,reference.out}"}
+    with open(os.path.join(here, "helical_mhdturb_ref.json"), "w") as fh:
+        json.dump({"params": hpar, "kdat": {"nk": nk, "kav": kav, "kxyz": kk}, "series": series}, fh, indent=1)
+
     with open(os.path.join(here, "var_subrecords.json"), "w") as fh:
         json.dump({"dim": [mx, my, mz, nv], "seed": 7, "max_subrecord": 1000, "file_bytes": size,
                    "ref_reader_sum": float(f2.sum()), "ref_reader_t": float(g2[0])}, fh, indent=1)

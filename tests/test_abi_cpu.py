@@ -83,6 +83,8 @@ def test_no_cpu_fallback_without_gpu(pc):
     p = pc.default_params(nx=16, ny=16, nz=16, dt=1e-3)
     with pytest.raises(pc.PcgbError):
         pc.Box(p)
+    # the C ABI records a sticky error (the Python layer clears it once raised)
+    assert not L.pcgb_box_create(C.byref(p))
     rc = L.pcgb_last_error()
     assert rc != 0 and L.pcgb_error_string(rc)
     # the plug-in path records an error and computes nothing
