@@ -11,7 +11,7 @@ src/param_io.f90:82-250, :461-570, restricted to the keys of this hot path:
   &entropy_run_pars     chi, iheatcond ('chi-const' only), lviscosity_heat
   &hydro_run_pars       lforcing_cont_uu, ampl_fcont_uu
   &forcing_run_pars     lforcing_cont, iforcing_cont ('ABC'), ampl_ff, k1_ff, kf_fcont, relhel,
-                        ABC_A, ABC_B, ABC_C
+                        ABC_A, ABC_B, ABC_C; iforce ('helical' or 'zero'), force
   &magnetic_init_pars   initaa, amplaa (initial condition, returned separately)
 
 Keys outside this set are kept in ``extra`` so a caller can see what was not applied.
@@ -151,6 +151,11 @@ def params_from_namelists(start_text: str, run_text: str, n=(32, 32, 32), lentro
     if cont and kinds and kinds[0] != "abc":
         raise ValueError(f"continuous forcing {kinds[0]!r}: only 'ABC' is implemented")
     p.lforcing_cont = int(cont)
+    iforce = str(fr.get("iforce", "zero")).strip().lower()
+    if iforce not in ("zero", "helical", "2"):
+        raise ValueError(f"iforce={iforce!r}: only 'helical' (and 'zero') are implemented")
+    p.lforcing_hel = int(iforce in ("helical", "2"))
+    take("forcing_run_pars", "force", lambda v: setattr(p, "force_hel", float(_first(v))))
     take("forcing_run_pars", "ampl_ff", lambda v: setattr(p, "ampl_ff", float(_first(v))))
     take("forcing_run_pars", "k1_ff", lambda v: setattr(p, "kf", float(_first(v))))
     take("forcing_run_pars", "kf_fcont", lambda v: setattr(p, "kf", float(_first(v))))
@@ -164,7 +169,7 @@ def params_from_namelists(start_text: str, run_text: str, n=(32, 32, 32), lentro
              "entropy_run_pars": {"chi", "iheatcond", "lviscosity_heat"},
              "hydro_run_pars": {"lforcing_cont_uu", "ampl_fcont_uu"},
              "forcing_run_pars": {"lforcing_cont", "iforcing_cont", "ampl_ff", "k1_ff", "kf_fcont", "relhel",
-                                  "abc_a", "abc_b", "abc_c"}}
+                                  "abc_a", "abc_b", "abc_c", "iforce", "force"}}
     for grp, keys in known.items():
         for k, v in g.get(grp, {}).items():
             if re.sub(r"\(.*\)$", "", k) not in keys:
@@ -174,3 +179,14 @@ def params_from_namelists(start_text: str, run_text: str, n=(32, 32, 32), lentro
     ic["nt"] = rp.get("nt")
     ic["it1"] = rp.get("it1", 10)
     return p, ic, extra
+
+
+def read_kdat(path: str):
+    """The wavevector list of the random helical forcing, the reference's k.dat
+    (forcing.f90:888-900): 'nk kav', then kkx, kky, kkz.  Returns ((3, nk) array, kav)
+    for Box.set_kvectors / pcgb_set_kvectors."""
+    import numpy as np
+    with open(path) as fh:
+        vals = fh.read().split()
+    nk, kav = int(vals[0]), float(vals[1])
+    return np.array([float(v) for v in vals[2:2 + 3 * nk]]).reshape(3, nk), kav

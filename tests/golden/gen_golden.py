@@ -18,8 +18,8 @@ nowhere else):
    and what the reference's own Fortran record reader
    (python/pencil/read/fortran_file.py, FortranFileExt) reads from it.
 5. helical_mhdturb_ref.json -- samples/helical-MHDturb: the wavevector list
-   k.dat (random helical forcing) and the it / t / dt / umax / urms columns of
-   reference.out, with the sample's run parameters.
+   k.dat (random helical forcing), the it / t / dt / umax / urms columns of
+   reference.out, the sample's run parameters and its start.in / run.in text.
 4. var_subrecords.json -- a small snapshot written by
    pencil-code_gb300/vardat.py with a tiny subrecord size, checked at
    generation time to read back identically through FortranFileExt.
@@ -162,8 +162,13 @@ def main(ref_root):
     hpar = {"n": 32, "gamma": 1.0, "nu": 5e-3, "eta": 5e-3, "iforce": "helical", "force": 0.07, "relhel": 1.0,
             "dt": 4e-2, "nt": 10, "it1": 2, "cdt": 0.4, "cdtv": 0.3,
             "source": "samples/helical-MHDturb/{start.in,run.in,k.dat,reference.out}"}
+    hnl = {}
+    for name in ("start.in", "run.in"):
+        with open(os.path.join(hdir, name)) as fh:
+            hnl[name] = fh.read()
     with open(os.path.join(here, "helical_mhdturb_ref.json"), "w") as fh:
-        json.dump({"params": hpar, "kdat": {"nk": nk, "kav": kav, "kxyz": kk}, "series": series}, fh, indent=1)
+        json.dump({"params": hpar, "kdat": {"nk": nk, "kav": kav, "kxyz": kk}, "series": series,
+                   "namelists": hnl}, fh, indent=1)
 
     with open(os.path.join(here, "var_subrecords.json"), "w") as fh:
         json.dump({"dim": [mx, my, mz, nv], "seed": 7, "max_subrecord": 1000, "file_bytes": size,

@@ -153,3 +153,25 @@ def test_namelist_unsupported_settings_are_errors():
                                      " iforcing_cont(1)='RobertsFlow' /")
     _, _, extra = nl.params_from_namelists("", "&viscosity_run_pars nu=0.01, nu_hyper3=1e-9 /")
     assert extra == {"viscosity_run_pars.nu_hyper3": 1e-9}
+
+
+def test_namelists_of_helical_mhdturb_sample(tmp_path):
+    ref = _json("helical_mhdturb_ref.json")
+    p, ic, extra = nl.params_from_namelists(ref["namelists"]["start.in"], ref["namelists"]["run.in"], n=(32,) * 3)
+    prm = ref["params"]
+    assert p.lforcing_hel == 1 and p.force_hel == prm["force"] and p.relhel == prm["relhel"]
+    assert p.nu == prm["nu"] and p.eta == prm["eta"] and p.dt == prm["dt"] and p.gamma == prm["gamma"]
+    assert p.cdt == prm["cdt"] and p.cdtv == prm["cdtv"] and ic["nt"] == prm["nt"]
+    assert "run_pars.random_gen" in extra
+    # k.dat written back in the reference's format reads the same
+    kd = ref["kdat"]
+    kk = np.array(kd["kxyz"]).reshape(3, kd["nk"])
+    path = tmp_path / "k.dat"
+    with open(path, "w") as fh:
+        fh.write(f"{kd['nk']} {kd['kav']}\n")
+        for row in kk:
+            fh.write(" ".join(str(int(v)) for v in row) + "\n")
+    k2, kav = nl.read_kdat(str(path))
+    assert kav == kd["kav"] and np.array_equal(k2, kk)
+    with pytest.raises(ValueError, match="iforce"):
+        nl.params_from_namelists("", "&forcing_run_pars iforce='irrotational' /")
