@@ -264,7 +264,9 @@ typedef struct pcgb_server pcgb_server;
 pcgb_server* pcgb_server_create(size_t mem_budget_bytes, int max_active, int round_steps);
 /* init: Gaussian noise of amplitude noise_ampl on aa (seeded), ABC flow of
    amplitude abc_ampl on uu when abc_ampl != 0.  f_out, if not NULL, receives
-   the final f(mx,my,mz,nf) (double, Fortran order).  Returns a request id >= 0. */
+   the final f(mx,my,mz,nf) (double, Fortran order).  Returns a request id >= 0,
+   or -1 for a bad request (requests with lforcing_hel are refused: that forcing
+   runs through the box API). */
 long long pcgb_server_submit(pcgb_server* s, const pcgb_params* p, int nsteps, unsigned long long seed,
                              double noise_ampl, double abc_ampl, double* f_out);
 /* 1 when request id is done (times[0..2] = submitted, started, finished;

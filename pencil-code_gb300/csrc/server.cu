@@ -208,6 +208,7 @@ extern "C" pcgb_server* pcgb_server_create(size_t mem_budget_bytes, int max_acti
 extern "C" long long pcgb_server_submit(pcgb_server* s, const pcgb_params* p, int nsteps, unsigned long long seed,
                                         double noise_ampl, double abc_ampl, double* f_out) {
   if (!s || !p || nsteps < 1) return -1;
+  if (p->lforcing_hel) return -1;   // the step-end helical forcing runs through the box API only
   Req* r = new Req();
   r->p = *p;
   // (16,8) tiles suit small boxes: packed pairs for FP32 and double-float, field-major for FP64
