@@ -319,8 +319,14 @@ def run_e2e(args, pc, gpu, torch, stream, p, nf, ws: int = 1):
         avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
     except Exception:
         avail = 0
-    # every rank of the node pins its own host f-array at the same time
-    if avail and nbytes > 0.45 * avail / max(ws, 1):
+    # every rank of the node pins its own host f-array at the same time; all ranks
+    # take the same decision (a collective follows)
+    fits = not (avail and nbytes > 0.45 * avail / max(ws, 1))
+    if ws > 1:
+        flag = torch.tensor([1 if fits else 0], dtype=torch.int32, device="cuda")
+        torch.distributed.all_reduce(flag, op=torch.distributed.ReduceOp.MIN)
+        fits = bool(flag.item())
+    if not fits:
         return {"value": None, "unit": "Gcell-updates/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                 "note": f"host f-array of {nbytes / 1e9:.1f} GB x {ws} ranks exceeds the host memory budget"}
     ht = torch.zeros(int(np.prod(shape)), dtype=torch.float64, pin_memory=True)
@@ -339,6 +345,8 @@ def run_e2e(args, pc, gpu, torch, stream, p, nf, ws: int = 1):
         for s in (1, 2, 3):
             L.substepGPU(s, 0.0)
     torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     gpu.load_farray_to_gpu()
     for _ in range(args.steps):
@@ -347,12 +355,13 @@ def run_e2e(args, pc, gpu, torch, stream, p, nf, ws: int = 1):
         L.getGPUReducedVars(rp)
     gpu.copy_farray_from_gpu(fh)
     torch.cuda.synchronize()
-    el = time.perf_counter() - t0
-    rc, msg = pc.lib.last_error() if hasattr(pc, "lib") else (0, "")
+    el = max_over_ranks(time.perf_counter() - t0, device="cuda")
     gpu.finalize_gpu()
     cells = float(n) ** 3
-    return {"value": cells * 3 * args.steps / el / 1e9, "unit": "Gcell-updates/s",
-            "h2d_bytes_per_step": nbytes / args.steps, "d2h_bytes_per_step": nbytes / args.steps + red.nbytes,
+    # whole job: every rank advances its own replica through its own host array
+    return {"value": ws * cells * 3 * args.steps / el / 1e9, "unit": "Gcell-updates/s",
+            "h2d_bytes_per_step": ws * nbytes / args.steps,
+            "d2h_bytes_per_step": ws * (nbytes / args.steps + red.nbytes),
             "what": "loadFarray + K x (substepGPU x3 + getGPUReducedVars) + copyFarray, pinned host f-array "
                     "(REAL=double), wall clock"}
 
