@@ -248,14 +248,19 @@ static int default_zdepth(const pcgb_box* b) {
   return zd;
 }
 
-// FP32: packed pairs on (32,8) tiles, one 8-warp CTA per SM; double-float:
-// packed pairs on (16,12) tiles, one 6-warp CTA per SM; FP64: one 6-warp CTA
-// per SM, (32,6) with 7 fields, (24,8) with 8 (an 8-field ring of (32,6)
-// planes needs 246 KB of shared memory)
-static int default_tile(int tb, int nf, int dfl) { return tb == 4 ? 5 : (dfl ? 5 : (nf == 8 ? 2 : 3)); }
+// FP32: packed pairs on (32,8) tiles, one 8-warp CTA per SM, when a box has
+// at least a wave of such column tiles, else on (16,8) tiles with two CTAs
+// per SM (more, smaller work items for small boxes); double-float: packed
+// pairs on (16,12) tiles, one 6-warp CTA per SM; FP64: one 6-warp CTA per SM,
+// (32,6) with 7 fields, (24,8) with 8 (an 8-field ring of (32,6) planes needs
+// 246 KB of shared memory)
+static int default_tile(int tb, int nf, int dfl, int nx, int ny) {
+  if (tb == 4) return ((long long)((nx + 31) / 32) * ((ny + 7) / 8) >= 152) ? 5 : 6;
+  return dfl ? 5 : (nf == 8 ? 2 : 3);
+}
 
 static int set_tiling(pcgb_box* b, int tile, int zd) {
-  if (tile < 0) tile = default_tile(b->tb, b->nf, b->dfl);
+  if (tile < 0) tile = default_tile(b->tb, b->nf, b->dfl, b->nx, b->ny);
   if (tile >= num_tiles(b->tb, b->dfl)) return set_err(PCGB_E_ARG, "tile variant %d out of range", tile);
   if ((int)tile_is_pair(b->tb, tile, b->dfl) != b->pairs)
     return set_err(PCGB_E_ARG, "tile %d needs a different device layout than this box was created with", tile);
@@ -320,7 +325,7 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   b->nx = p->nx; b->ny = p->ny; b->nz = p->nz;
   b->mx = p->nx + 6; b->my = p->ny + 6; b->mz = p->nz + 6;
   {
-    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb, b->nf, b->dfl);
+    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb, b->nf, b->dfl, p->nx, p->ny);
     b->pairs = (t0 < num_tiles(b->tb, b->dfl) && tile_is_pair(b->tb, t0, b->dfl)) ? 1 : 0;
   }
   b->eb = b->pairs ? (b->dfl ? 16 : 8) : b->tb;
@@ -375,7 +380,7 @@ extern "C" size_t pcgb_params_bytes(const pcgb_params* p) {
   if (!p || p->nx < 1 || p->ny < 1 || p->nz < 1 || (p->precision != 4 && p->precision != 8)) return 0;
   const int tb = p->precision, nf = p->lentropy ? 8 : 7;
   const int dfl = (tb == 8 && p->dfloat) ? 1 : 0;
-  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb, nf, dfl);
+  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb, nf, dfl, p->nx, p->ny);
   const int pairs = (t0 < num_tiles(tb, dfl) && tile_is_pair(tb, t0, dfl)) ? 1 : 0;
   const int eb = pairs ? (dfl ? 16 : 8) : tb, ns = pairs ? 4 : nf;
   const int xoff = 128 / eb;
