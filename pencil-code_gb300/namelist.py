@@ -178,6 +178,7 @@ def params_from_namelists(start_text: str, run_text: str, n=(32, 32, 32), lentro
     ic.update({f"hydro.{k}": v for k, v in sg.get("hydro_init_pars", {}).items()})
     ic["nt"] = rp.get("nt")
     ic["it1"] = rp.get("it1", 10)
+    ic["dsnap"] = float(_first(rp.get("dsnap", 0.0)))
     return p, ic, extra
 
 
