@@ -96,7 +96,7 @@ def run(start_text: str, run_text: str, n, outdir: str, kdat=None, precision: in
                 rows.append(row)
                 series.write(format_series_row(row) + "\n")
                 series.flush()
-            if t >= tsnap:   # wsnap: one snapshot per crossing of a multiple of dsnap
+            if t >= tsnap:   # wsnap (snapshot.f90:265): one snapshot per crossing of a multiple of dsnap
                 isnap += 1
                 path = os.path.join(proc, f"VAR{isnap}")
                 write_box_snapshot(path, p, box.store(), t)
