@@ -69,6 +69,11 @@ typedef struct pcgb_params {
                               after every step; wavevectors from pcgb_box_set_kvectors / pcgb_set_kvectors */
   int seed_ff;             /* seed of the forcing's random stream (ran0, general.f90:867) */
   double force_hel;        /* &forcing_run_pars force (amplitude of the helical forcing) */
+  int lupw_uu;             /* &hydro_run_pars lupw_uu: upwinded u.grad u (5th-order correction) */
+  int lupw_lnrho;          /* &density_run_pars lupw_lnrho: upwinded u.grad lnrho */
+  int lmagnetic_forcing;   /* &forcing_run_pars lmagnetic_forcing with iforce='helical': the force goes
+                              into aa and a second, independent force into uu (forcing.f90:314-340) */
+  int pad_;
 } pcgb_params;
 
 /* Defaults of the reference (cdata.f90:211,235,239; eos_idealgas.f90:47;

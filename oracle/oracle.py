@@ -37,6 +37,7 @@ class OrcParams(C.Structure):
         ("b_ext", C.c_double * 3),
         ("lohmic_heat", C.c_int), ("lviscosity_heat", C.c_int),
         ("cdt", C.c_double), ("cdtv", C.c_double),
+        ("lupw_uu", C.c_int), ("lupw_lnrho", C.c_int),
     ]
 
 
@@ -81,7 +82,7 @@ def lib():
         L.orc_grid.argtypes = [P, dpc, dpc, dpc]
         L.orc_helical_coefs.argtypes = [P, C.c_double, dpc, dpc, dpc, C.c_int, C.c_double, C.POINTER(C.c_int),
                                         C.POINTER(HelRec)]
-        L.orc_add_helical.argtypes = [P, dp, C.POINTER(HelRec), C.c_double]
+        L.orc_add_helical.argtypes = [P, dp, C.POINTER(HelRec), C.c_double, C.c_int]
         _lib = L
     return _lib
 
@@ -95,7 +96,7 @@ def make_params(**kw) -> OrcParams:
              gamma=1.0, cs0=1.0, rho0=1.0, cp=1.0, nu=0.0, eta=0.0, chi=0.0, mu0=1.0,
              lforcing_cont=0, ampl_ff=0.0, kf=1.0, relhel=1.0, abc_a=1.0, abc_b=1.0, abc_c=1.0,
              ampl_fcont_uu=1.0, b_ext=(0.0, 0.0, 0.0), lohmic_heat=1, lviscosity_heat=1,
-             cdt=0.9, cdtv=0.25)
+             cdt=0.9, cdtv=0.25, lupw_uu=0, lupw_lnrho=0)
     d.update(kw)
     p = OrcParams()
     for k, v in d.items():
@@ -164,9 +165,10 @@ def helical_coefs(p: OrcParams, force: float, kvec: np.ndarray, kav: float, stat
     return rec, s.value
 
 
-def add_helical(p: OrcParams, f: np.ndarray, rec: HelRec, dt: float) -> None:
-    """forcing_hel: f(uu) += the step's helical forcing (interior; refresh ghosts after)."""
-    lib().orc_add_helical(C.byref(p), f, C.byref(rec), dt)
+def add_helical(p: OrcParams, f: np.ndarray, rec: HelRec, dt: float, target: int = 0) -> None:
+    """forcing_hel: f(uu) (target 0) or f(aa) (target 1) += the step's helical
+    forcing (interior; refresh ghosts after)."""
+    lib().orc_add_helical(C.byref(p), f, C.byref(rec), dt, target)
 
 
 def read_kdat(path: str):

@@ -169,6 +169,22 @@ static inline double derij_c(const ctx_t* c, const double* f, int k, int i, int 
   return fac * ((270.0 * t[0] - 27.0 * t[1]) + 2.0 * t[2]);
 }
 
+/* der6_main with upwind=T (deriv.f90:936-1010): the 6th difference times
+   dx_1/60, (1/60) dx_1 (-20 f0 + 15 (f1 + f-1) - 6 (f2 + f-2) + (f3 + f-3)). */
+static inline double der6_upwind_c(const ctx_t* c, const double* f, int k, int j, int l, int m, int n) {
+  size_t s = (j == 0) ? 1 : (j == 1) ? (size_t)c->mx : (size_t)c->mx * c->my;
+  const double fac = (j == 0) ? (1.0 / 60.0) * c->dx_1 : (j == 1) ? (1.0 / 60.0) * c->dy_1 : (1.0 / 60.0) * c->dz_1;
+  const double* q = f + IDX(c, l, m, n, k);
+  const ptrdiff_t a = (ptrdiff_t)s, b = 2 * (ptrdiff_t)s, d = 3 * (ptrdiff_t)s;
+  return fac * (((-20.0 * q[0] + 15.0 * (q[a] + q[-a])) - 6.0 * (q[b] + q[-b])) + (q[d] + q[-d]));
+}
+
+/* calc_del6_for_upwind (sub.f90:7491-7539): sum_j |u_j| der6_j(f_k, upwind). */
+static inline double del6_upwind(const ctx_t* c, const double* f, int k, const double uu[3], int l, int m, int n) {
+  return (fabs(uu[0]) * der6_upwind_c(c, f, k, 0, l, m, n) + fabs(uu[1]) * der6_upwind_c(c, f, k, 1, l, m, n)) +
+         fabs(uu[2]) * der6_upwind_c(c, f, k, 2, l, m, n);
+}
+
 double orc_der(const orc_params* p, const double* f, int k, int j, int l, int m, int n) {
   ctx_t c; ctx_init(&c, p); double r = der_c(&c, f, k, j, l, m, n); ctx_free(&c); return r;
 }
@@ -225,9 +241,13 @@ static double cell(const orc_params* p, const ctx_t* c, const double* f, double*
     sij2 = sij2 + sij[i][i] * sij[i][i];
     for (int j = 0; j < i; ++j) sij2 = sij2 + 2.0 * (sij[i][j] * sij[i][j]);
   }
-  /* ugu: u_dot_grad_vec -> dot_mn(uu, uij(:,j,:)), sub.f90:3482/:599 */
+  /* ugu: u_dot_grad_vec -> dot_mn(uu, uij(:,j,:)), sub.f90:3482/:599;
+     with lupw_uu, minus the upwind correction (doupwind, sub.f90:7541) */
   double ugu[3];
-  for (int j = 0; j < 3; ++j) ugu[j] = (uu[0] * uij[j][0] + uu[1] * uij[j][1]) + uu[2] * uij[j][2];
+  for (int j = 0; j < 3; ++j) {
+    ugu[j] = (uu[0] * uij[j][0] + uu[1] * uij[j][1]) + uu[2] * uij[j][2];
+    if (p->lupw_uu) ugu[j] = ugu[j] - del6_upwind(c, f, iux + j, uu, l, m, n);
+  }
   /* del2u, graddivu: del2v_etc, sub.f90:2610 */
   double fijj[3][3], fjji[3][3];
   for (int i = 0; i < 3; ++i)
@@ -246,6 +266,7 @@ static double cell(const orc_params* p, const ctx_t* c, const double* f, double*
   double glnrho[3];
   for (int j = 0; j < 3; ++j) glnrho[j] = der_c(c, f, ilnrho, j, l, m, n);
   double uglnrho = (uu[0] * glnrho[0] + uu[1] * glnrho[1]) + uu[2] * glnrho[2];
+  if (p->lupw_lnrho) uglnrho = uglnrho - del6_upwind(c, f, ilnrho, uu, l, m, n);   /* density.f90:2772 */
   double sglnrho[3];
   for (int i = 0; i < 3; ++i)   /* multmv_mn, sub.f90:1228 */
     sglnrho[i] = (sij[i][0] * glnrho[0] + sij[i][1] * glnrho[1]) + sij[i][2] * glnrho[2];
@@ -541,8 +562,9 @@ void orc_helical_coefs(const orc_params* p, double force, const double* kkx, con
 /* forcing_hel, forcing.f90:2066-2474, default path, with fxyz_coefs_hel
    (:1882-1930): fx = exp(i(kx k1 x + phase)) fact, fy = exp(i ky k1 y),
    fz = exp(i kz k1 z); f(uu_j) += Re[(coef1_j + i coef2_j) (fx fy) fz]. */
-void orc_add_helical(const orc_params* p, double* f, const orc_helrec* rec, double dt) {
+void orc_add_helical(const orc_params* p, double* f, const orc_helrec* rec, double dt, int target) {
   const int mx = p->nx + 2 * NG, my = p->ny + 2 * NG, mz = p->nz + 2 * NG;
+  const int j0 = target ? (p->lentropy ? 5 : 4) : 0;   /* iax or iux, 0-based */
   const double fact = rec->fact0 * sqrt(dt);
   const double k1 = p->kf;
   double* x = malloc(sizeof(double) * (mx + my + mz));
@@ -561,7 +583,7 @@ void orc_add_helical(const orc_params* p, double* f, const orc_helrec* rec, doub
         const double pr = fxr * fyr - fxi * fyi, pim = fxr * fyi + fxi * fyr;   /* fx fy */
         const double qr = pr * fzr - pim * fzi, qi = pr * fzi + pim * fzr;      /* (fx fy) fz */
         for (int j = 0; j < 3; ++j) {
-          const size_t o = (size_t)l + (size_t)mx * ((size_t)m + (size_t)my * ((size_t)n + (size_t)mz * j));
+          const size_t o = (size_t)l + (size_t)mx * ((size_t)m + (size_t)my * ((size_t)n + (size_t)mz * (j0 + j)));
           f[o] = f[o] + (rec->coef1[j] * qr - rec->coef2[j] * qi);
         }
       }

@@ -32,6 +32,7 @@ typedef struct {
   double b_ext[3];
   int lohmic_heat, lviscosity_heat;
   double cdt, cdtv;
+  int lupw_uu, lupw_lnrho;  /* upwinded advection (hydro.f90:3662, density.f90:2772) */
 } orc_params;
 
 /* Diagnostic slots (FP64), evaluated on f at the start of a step. */
@@ -82,8 +83,9 @@ typedef struct {
 } orc_helrec;
 void orc_helical_coefs(const orc_params* p, double force, const double* kkx, const double* kky, const double* kkz,
                        int nk, double kav, int* state, orc_helrec* rec);
-/* f(uu) += forcing over the interior (ghosts are the caller's to refresh). */
-void orc_add_helical(const orc_params* p, double* f, const orc_helrec* rec, double dt);
+/* f(uu) (target 0) or f(aa) (target 1, magnetic forcing) += forcing over the
+   interior (ghosts are the caller's to refresh). */
+void orc_add_helical(const orc_params* p, double* f, const orc_helrec* rec, double dt, int target);
 
 /* The reference 'min_std' generator ran0 (src/general.f90:867-889) and
    gaunoise_vect (src/initcond.f90:5005-5047). */

@@ -16,7 +16,8 @@
 
 namespace pcgb {
 
-template <int NF, int TX, int TY>
+// UPW: compiled with the upwind corrections (lupw_uu, lupw_lnrho).
+template <int NF, int TX, int TY, bool UPW = false>
 struct DDPairCell {
   using T = dd;
   using Elem = dd2;
@@ -64,6 +65,28 @@ struct DDPairCell {
       }
       return dd2_splat(fac) * (((c0 * f0 + c1 * s1) + c2 * s2) + c3 * s3);
     }
+    // der6_main with upwind=T, deriv.f90:936-1010, in ScalarCell::St::del6u's order
+    __device__ __forceinline__ dd2 del6u(int p, int j) const {
+      const dd2 f0 = v(0, p, 0, 0);
+      dd2 s1, s2, s3;
+      dd fac;
+      if (j == 0) {
+        s1 = v(0, p, 0, 1) + v(0, p, 0, -1); s2 = v(0, p, 0, 2) + v(0, p, 0, -2); s3 = v(0, p, 0, 3) + v(0, p, 0, -3);
+        fac = F.fx;
+      } else if (j == 1) {
+        s1 = v(0, p, 1, 0) + v(0, p, -1, 0); s2 = v(0, p, 2, 0) + v(0, p, -2, 0); s3 = v(0, p, 3, 0) + v(0, p, -3, 0);
+        fac = F.fy;
+      } else {
+        s1 = v(1, p, 0, 0) + v(-1, p, 0, 0); s2 = v(2, p, 0, 0) + v(-2, p, 0, 0); s3 = v(3, p, 0, 0) + v(-3, p, 0, 0);
+        fac = F.fz;
+      }
+      return dd2_splat(fac) * (((dd2_scale(f0, -20.f) + dd2_scale(s1, 15.f)) - dd2_scale(s2, 6.f)) + s3);
+    }
+    // calc_del6_for_upwind, sub.f90:7491-7539, for the first member of pair p
+    __device__ __forceinline__ dd upwind(int p, const dd u[3]) const {
+      return (tabs(u[0]) * dd2_lane0(del6u(p, 0)) + tabs(u[1]) * dd2_lane0(del6u(p, 1))) +
+             tabs(u[2]) * dd2_lane0(del6u(p, 2));
+    }
     // derij_main bidiagonal, deriv.f90:1387-1447; pr: 0 = xy, 1 = yz, 2 = xz
     __device__ __forceinline__ dd2 derij(int p, int pr) const {
       dd2 t[3];
@@ -94,6 +117,7 @@ struct DDPairCell {
     const dd* cosz;
     dd fsz, fcz;   // sin/cos(kf z) of the current plane, prefetched one plane ahead
     dd2 dfnext[4];
+    int upw;       // UPW_* bits
 
     __device__ __forceinline__ void begin(const PcgbBoxDev& B, int inb, int x, int y, int z0, bool active,
                                           bool mode_cfl, const StepFlags<dd>& fl) {
@@ -103,6 +127,7 @@ struct DDPairCell {
       dfp = reinterpret_cast<dd2*>(B.df);
       ps = B.ps; fs = B.fs; px = B.px; xoff = B.xoff; nx = B.nx; ny = B.ny; nz = B.nz;
       forcing = B.lforcing != 0; iso = B.isothermal != 0; vheat = B.lviscosity_heat != 0; oheat = B.lohmic_heat != 0;
+      upw = UPW ? B.lupw : 0;
       const dd* sinx = reinterpret_cast<const dd*>(B.forc);
       const dd* cosx = sinx + B.px;
       const dd* siny = cosx + B.px;
@@ -199,6 +224,13 @@ struct DDPairCell {
       }
       CellIn<dd> c;
       gather(st, c, fl.want_diag);
+      if constexpr (UPW) {
+        if (upw & UPW_UU) {
+#pragma unroll
+          for (int p = 0; p < 3; ++p) c.upw_u[p] = st.upwind(p, c.uu);
+        }
+        if (upw & UPW_LNRHO) c.upw_lnrho = st.upwind(3, c.uu);
+      }
       dd fc[3] = {dd(0), dd(0), dd(0)};
       if (forcing) {   // forcing_cont 'ABC', forcing.f90:5894-5896
         fc[0] = P.fact * (P.abc_c * fsz + (P.fact2 * P.abc_b) * fcy);
@@ -215,7 +247,7 @@ struct DDPairCell {
       dfo[ILNRHO] = dd2_lane0(dfo2[3]);
       if (ENTROPY) dfo[ISS] = dd2_lane1(dfo2[3]);
       cell_rhs<dd, NF>(c, P, F, fc, forcing, iso, vheat, oheat, dfo, fl.alpha, dfn, fl.want_cfl, fl.want_diag, acc,
-                       dt1max);
+                       dt1max, UPW ? upw : 0);
 
       // ---- 2N update (timestep.f90:160), per pair, in ScalarCell's order ----
       dd2 dn[4];

@@ -20,7 +20,8 @@ __device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(
 __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 p_splat(float v) { return make_float2(v, v); }
 
-template <int NF, int TX, int TY>
+// UPW: compiled with the upwind corrections (lupw_uu, lupw_lnrho).
+template <int NF, int TX, int TY, bool UPW = false>
 struct PairCell {
   using T = float;
   using Elem = float2;
@@ -72,6 +73,29 @@ struct PairCell {
       t = p_fma(p_splat((float)(2.0 / 180.0)), s3, t);
       return p_mul(p_splat(fac), t);
     }
+    // der6_main with upwind=T (deriv.f90:936-1010) on both members of pair p
+    __device__ __forceinline__ float2 del6u(int p, int j) const {
+      float2 s1, s2, s3;
+      float fac;
+      if (j == 0) {
+        s1 = p_add(v(0, p, 0, 1), v(0, p, 0, -1)); s2 = p_add(v(0, p, 0, 2), v(0, p, 0, -2));
+        s3 = p_add(v(0, p, 0, 3), v(0, p, 0, -3)); fac = F.fx;
+      } else if (j == 1) {
+        s1 = p_add(v(0, p, 1, 0), v(0, p, -1, 0)); s2 = p_add(v(0, p, 2, 0), v(0, p, -2, 0));
+        s3 = p_add(v(0, p, 3, 0), v(0, p, -3, 0)); fac = F.fy;
+      } else {
+        s1 = p_add(v(1, p, 0, 0), v(-1, p, 0, 0)); s2 = p_add(v(2, p, 0, 0), v(-2, p, 0, 0));
+        s3 = p_add(v(3, p, 0, 0), v(-3, p, 0, 0)); fac = F.fz;
+      }
+      float2 t = p_mul(p_splat(-20.f), v(0, p, 0, 0));
+      t = p_fma(p_splat(15.f), s1, t);
+      t = p_fma(p_splat(-6.f), s2, t);
+      return p_mul(p_splat(fac), p_add(t, s3));
+    }
+    // calc_del6_for_upwind (sub.f90:7491-7539) for the first member of pair p: sum_j |u_j| D6_j
+    __device__ __forceinline__ float upwind(int p, const float u[3]) const {
+      return (fabsf(u[0]) * del6u(p, 0).x + fabsf(u[1]) * del6u(p, 1).x) + fabsf(u[2]) * del6u(p, 2).x;
+    }
     // derij_main bidiagonal (deriv.f90:1387-1447); (a,b) with a<b: 0=x,1=y,2=z
     __device__ __forceinline__ float2 derij(int p, int a, int b) const {
       float2 t[3];
@@ -103,6 +127,7 @@ struct PairCell {
     const float* cosz;
     float fsz, fcz;   // sin/cos(kf z) of the current plane, prefetched one plane ahead
     float2 dfnext[4];
+    int upw;          // UPW_* bits
 
     __device__ __forceinline__ void begin(const PcgbBoxDev& B, int inb, int x, int y, int z0, bool active,
                                           bool mode_cfl, const StepFlags<float>& fl) {
@@ -112,6 +137,7 @@ struct PairCell {
       dfp = reinterpret_cast<float2*>(B.df);
       ps = B.ps; fs = B.fs; px = B.px; xoff = B.xoff; nx = B.nx; ny = B.ny; nz = B.nz;
       forcing = B.lforcing != 0; iso = B.isothermal != 0; vheat = B.lviscosity_heat != 0; oheat = B.lohmic_heat != 0;
+      upw = UPW ? B.lupw : 0;
       const float* sinx = reinterpret_cast<const float*>(B.forc);
       const float* cosx = sinx + B.px;
       const float* siny = cosx + B.px;
@@ -198,6 +224,13 @@ struct PairCell {
       } else {
         c.del2lnrho = c.del2ss = 0.f;
       }
+      if constexpr (UPW) {
+        if (upw & UPW_UU) {
+#pragma unroll
+          for (int p = 0; p < 3; ++p) c.upw_u[p] = st.upwind(p, c.uu);
+        }
+        if (upw & UPW_LNRHO) c.upw_lnrho = st.upwind(3, c.uu);
+      }
       float fc[3] = {0.f, 0.f, 0.f};
       if (forcing) {   // forcing_cont 'ABC', forcing.f90:5894-5896
         fc[0] = P.fact * (P.abc_c * fsz + (P.fact2 * P.abc_b) * fcy);
@@ -210,7 +243,7 @@ struct PairCell {
       if (ENTROPY) dfo[ISS] = dfo2[3].y;
       dfo[IAX] = dfo2[0].y; dfo[IAX + 1] = dfo2[1].y; dfo[IAX + 2] = dfo2[2].y;
       cell_rhs<float, NF>(c, P, F, fc, forcing, iso, vheat, oheat, dfo, fl.alpha, dfn, fl.want_cfl, fl.want_diag,
-                          acc, dt1max);
+                          acc, dt1max, UPW ? upw : 0);
 
       // ---- 2N update (timestep.f90:160), compensated in FP32, per pair ----
       float2 dn[4];

@@ -19,14 +19,19 @@ struct CellIn {
   T a2[3][3];                    // a2[i][j] = A_i,jj (der2)
   T a1xy, a2xy, a1xz, a3xz, a2yz, a3yz;   // mixed derivatives entering J
   T a3xy, a2xz, a1yz;                     // entering only the diagonal b_ii (div B)
+  T upw_u[3], upw_lnrho;                  // upwind corrections sum_j |u_j| D6_j f (lupw_uu, lupw_lnrho)
 };
+
+// Upwinding flags (bits of PcgbBoxDev::lupw): hydro.f90:3662 lupw_uu, density.f90:2772 lupw_lnrho.
+enum { UPW_UU = 1, UPW_LNRHO = 2 };
 
 // RHS of one cell in the order of calc_all_rhs (equ.f90:1268-1274).
 // dfo: df before the substep (already read); dfn: alpha*dfo + RHS.
 template <typename T, int NF>
 __device__ __forceinline__ void cell_rhs(const CellIn<T>& c, const Phys<T>& P, const Fac<T>& F, const T fc[3],
                                          bool forcing, bool iso, bool vheat, bool oheat, const T dfo[NF], T alpha,
-                                         T dfn[NF], bool want_cfl, bool want_diag, Acc& acc, T& dt1max) {
+                                         T dfn[NF], bool want_cfl, bool want_diag, Acc& acc, T& dt1max,
+                                         int upw = 0) {
   constexpr int IUX = 0, ILNRHO = 3, ISS = 4, IAX = NF - 3;
   constexpr bool ENTROPY = (NF == 8);
   const T(&uu)[3] = c.uu;
@@ -47,9 +52,14 @@ __device__ __forceinline__ void cell_rhs(const CellIn<T>& c, const Phys<T>& P, c
   T ugu[3];                                                              // u_dot_grad_vec, sub.f90:3482
 #pragma unroll
   for (int jj = 0; jj < 3; ++jj) ugu[jj] = (uu[0] * uij[jj][0] + uu[1] * uij[jj][1]) + uu[2] * uij[jj][2];
+  if (upw & UPW_UU) {                                                    // doupwind, sub.f90:7541
+#pragma unroll
+    for (int jj = 0; jj < 3; ++jj) ugu[jj] = ugu[jj] - c.upw_u[jj];
+  }
   // ---- density pencils (density.f90:2747-2800) ----
   const T rho1 = texp(-c.lnrho);
-  const T uglnrho = (uu[0] * c.glnrho[0] + uu[1] * c.glnrho[1]) + uu[2] * c.glnrho[2];
+  T uglnrho = (uu[0] * c.glnrho[0] + uu[1] * c.glnrho[1]) + uu[2] * c.glnrho[2];
+  if (upw & UPW_LNRHO) uglnrho = uglnrho - c.upw_lnrho;                // density.f90:2772
   T sglnrho[3];                                                          // multmv_mn, sub.f90:1228
 #pragma unroll
   for (int i = 0; i < 3; ++i) sglnrho[i] = (sij[i][0] * c.glnrho[0] + sij[i][1] * c.glnrho[1]) + sij[i][2] * c.glnrho[2];

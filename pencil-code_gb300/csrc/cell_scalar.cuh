@@ -7,7 +7,9 @@
 
 namespace pcgb {
 
-template <typename TT, int NF, int TX, int TY>
+// UPW: compiled with the upwind corrections (lupw_uu, lupw_lnrho); the
+// variants without them keep the registers of the plain advection terms.
+template <typename TT, int NF, int TX, int TY, bool UPW = false>
 struct ScalarCell {
   using T = TT;
   using Elem = TT;
@@ -45,6 +47,22 @@ struct ScalarCell {
       return F.sz * (((c0 * f0 + c1 * (v(1, k, 0, 0) + v(-1, k, 0, 0))) + c2 * (v(2, k, 0, 0) + v(-2, k, 0, 0))) +
                      c3 * (v(3, k, 0, 0) + v(-3, k, 0, 0)));
     }
+    // der6_main with upwind=T, deriv.f90:936-1010: (1/60) dx_1 (-20 f0 + 15 (f1 + f-1) - 6 (f2 + f-2) + (f3 + f-3))
+    __device__ __forceinline__ T del6u(int k, int j) const {
+      const T f0 = v(0, k, 0, 0);
+      if (j == 0)
+        return F.fx * (((wmul<T>(-20, f0) + wmul<T>(15, v(0, k, 0, 1) + v(0, k, 0, -1))) -
+                        wmul<T>(6, v(0, k, 0, 2) + v(0, k, 0, -2))) + (v(0, k, 0, 3) + v(0, k, 0, -3)));
+      if (j == 1)
+        return F.fy * (((wmul<T>(-20, f0) + wmul<T>(15, v(0, k, 1, 0) + v(0, k, -1, 0))) -
+                        wmul<T>(6, v(0, k, 2, 0) + v(0, k, -2, 0))) + (v(0, k, 3, 0) + v(0, k, -3, 0)));
+      return F.fz * (((wmul<T>(-20, f0) + wmul<T>(15, v(1, k, 0, 0) + v(-1, k, 0, 0))) -
+                      wmul<T>(6, v(2, k, 0, 0) + v(-2, k, 0, 0))) + (v(3, k, 0, 0) + v(-3, k, 0, 0)));
+    }
+    // calc_del6_for_upwind, sub.f90:7491-7539: sum_j |u_j| D6_j f
+    __device__ __forceinline__ T upwind(int k, const T u[3]) const {
+      return (tabs(u[0]) * del6u(k, 0) + tabs(u[1]) * del6u(k, 1)) + tabs(u[2]) * del6u(k, 2);
+    }
     // derij_main bidiagonal, deriv.f90:1387-1447; (a,b) with a<b: 0=x,1=y,2=z
     __device__ __forceinline__ T derij(int k, int a, int b) const {
       T t[3];
@@ -75,6 +93,7 @@ struct ScalarCell {
     const T* cosz;
     T fsz, fcz;   // sin/cos(kf z) of the current plane, prefetched one plane ahead
     T dfnext[NF];
+    int upw;      // UPW_* bits
 
     __device__ __forceinline__ void begin(const PcgbBoxDev& B, int inb, int x, int y, int z0, bool active,
                                           bool mode_cfl, const StepFlags<T>& fl) {
@@ -84,6 +103,7 @@ struct ScalarCell {
       dfp = reinterpret_cast<T*>(B.df);
       ps = B.ps; fs = B.fs; px = B.px; xoff = B.xoff; nx = B.nx; ny = B.ny; nz = B.nz;
       forcing = B.lforcing != 0; iso = B.isothermal != 0; vheat = B.lviscosity_heat != 0; oheat = B.lohmic_heat != 0;
+      upw = UPW ? B.lupw : 0;
       const T* sinx = reinterpret_cast<const T*>(B.forc);
       const T* cosx = sinx + B.px;
       const T* siny = cosx + B.px;
@@ -105,6 +125,14 @@ struct ScalarCell {
     }
 
     // Field values and stencil derivatives of one cell, fully unrolled.
+    static __device__ __forceinline__ void upwinding(const St& st, CellIn<T>& c, int upw) {
+      if (upw & UPW_UU) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) c.upw_u[i] = st.upwind(IUX + i, c.uu);
+      }
+      if (upw & UPW_LNRHO) c.upw_lnrho = st.upwind(ILNRHO, c.uu);
+    }
+
     static __device__ __forceinline__ void gather(const St& st, CellIn<T>& c, bool want_diag) {
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
@@ -249,6 +277,9 @@ struct ScalarCell {
       CellIn<T> c;
       if constexpr (is_dd<T>::value) gather_compact(st, c, fl.want_diag);
       else gather(st, c, fl.want_diag);
+      if constexpr (UPW) {
+        if (upw) upwinding(st, c, upw);
+      }
       T fc[3] = {T(0), T(0), T(0)};
       if (forcing) {   // forcing_cont 'ABC', forcing.f90:5894-5896
         fc[0] = P.fact * (P.abc_c * fsz + (P.fact2 * P.abc_b) * fcy);
@@ -258,7 +289,7 @@ struct ScalarCell {
       }
       T dfn[NF];
       cell_rhs<T, NF>(c, P, F, fc, forcing, iso, vheat, oheat, dfo, fl.alpha, dfn, fl.want_cfl, fl.want_diag, acc,
-                      dt1max);
+                      dt1max, UPW ? upw : 0);
 
       // ---- 2N update (timestep.f90:160) and periodic ghost images ----
       T fnew[NF], dsto[NF];

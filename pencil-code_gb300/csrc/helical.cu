@@ -4,7 +4,8 @@
 // polarisation vectors, fda = 1, unit profiles, slope_ff = 0, cs0eff = cs0.
 //
 // After every time step the force, a single helical Fourier mode of the
-// wavevector list, is added to uu as an Euler step (constant over the step):
+// wavevector list, is added to uu (to aa with lmagnetic_forcing) as an Euler
+// step (constant over the step):
 //   uu_j += Re[(coef1_j + i coef2_j) fx(x) fy(y) fz(z)],
 //   fx = exp(i(kx k1 x + phase)) force/ffnorm sqrt(dt), fy = exp(i ky k1 y),
 //   fz = exp(i kz k1 z).
@@ -108,42 +109,55 @@ __device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
 
-// uu_j element e (units of the layout's element) += v
+// component c of uu (target 0) or aa (target 1) at cell `cell` += v
 template <int LAYOUT, typename R>
-__device__ __forceinline__ void add_u(void* f, long long e, R v) {
-  if (LAYOUT == HEL_F32) {
-    float* p = static_cast<float*>(f) + e;
-    *p = radd(*p, (float)v);
-  } else if (LAYOUT == HEL_F64) {
-    double* p = static_cast<double*>(f) + e;
-    *p = radd(*p, (double)v);
-  } else if (LAYOUT == HEL_F32_PAIR) {
-    float* p = static_cast<float*>(f) + 2 * e;   // lane 0 of the (u, A) pair
-    *p = radd(*p, (float)v);
+__device__ __forceinline__ void add_field(void* f, const HelGeom& g, int target, int c, long long cell, R v) {
+  if (LAYOUT == HEL_F32 || LAYOUT == HEL_F64 || LAYOUT == HEL_DD) {
+    const long long e = (long long)(target ? g.iax + c : c) * g.fs + cell;   // field-major slice
+    if (LAYOUT == HEL_F32) {
+      float* p = static_cast<float*>(f) + e;
+      *p = radd(*p, (float)v);
+    } else if (LAYOUT == HEL_F64) {
+      double* p = static_cast<double*>(f) + e;
+      *p = radd(*p, (double)v);
+    } else {
+      float* p = static_cast<float*>(f) + 2 * e;   // (hi, lo)
+      const dd w(__dadd_rn((double)p[0] + (double)p[1], (double)v));
+      p[0] = w.hi;
+      p[1] = w.lo;
+    }
   } else {
-    float* p = static_cast<float*>(f) + (LAYOUT == HEL_DD ? 2 * e : 4 * e);
-    const int lo = (LAYOUT == HEL_DD) ? 1 : 2;   // dd: (hi, lo); dd2 lane 0: hi at 0, lo at 2
-    const dd w(__dadd_rn((double)p[0] + (double)p[lo], (double)v));
-    p[0] = w.hi;
-    p[lo] = w.lo;
+    const long long e = (long long)c * g.fs + cell;   // pair (u_c, A_c), lane = target
+    if (LAYOUT == HEL_F32_PAIR) {
+      float* p = static_cast<float*>(f) + 2 * e + target;
+      *p = radd(*p, (float)v);
+    } else {
+      float* p = static_cast<float*>(f) + 4 * e + target;   // dd2: hi lanes at 0, 1; lo lanes at 2, 3
+      const dd w(__dadd_rn((double)p[0] + (double)p[2], (double)v));
+      p[0] = w.hi;
+      p[2] = w.lo;
+    }
   }
 }
 
+// forcing_hel with lmagnetic_forcing (forcing.f90:318-345, :2289-2311): the
+// force goes into aa; uu receives forcing_rhs2 = Re[i coef3 fxyz] with coef3 =
+// crosshel k (k x (k x e)) (:1968, :2276-2281), zero for the default crosshel = 0,
+// so it is not applied.
 template <int LAYOUT, typename R>
 __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
-  const double* fx = tab + 8;
-  const double* fy = fx + 2 * g.nx;
-  const double* fz = fy + 2 * g.ny;
-  R c1[3], c2[3];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) { c1[j] = (R)tab[j]; c2[j] = (R)tab[3 + j]; }
   const long long total = (long long)g.nx * g.ny * g.nz;
+  const int target = g.magnetic ? 1 : 0;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(q % g.nx);
     const long long rr = q / g.nx;
     const int j = (int)(rr % g.ny);
     const int k = (int)(rr / g.ny);
+    const Images ix(i, g.nx), iy(j, g.ny), iz(k, g.nz);
+    const double* fx = tab + 8;
+    const double* fy = fx + 2 * g.nx;
+    const double* fz = fy + 2 * g.ny;
     const R xr = (R)fx[2 * i], xi = (R)fx[2 * i + 1];
     const R yr = (R)fy[2 * j], yi = (R)fy[2 * j + 1];
     const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
@@ -151,14 +165,14 @@ __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
     const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
     R fc[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) fc[c] = rsub(rmul(c1[c], qr), rmul(c2[c], qi));
-    const Images ix(i, g.nx), iy(j, g.ny), iz(k, g.nz);
+    for (int c = 0; c < 3; ++c) fc[c] = rsub(rmul((R)tab[c], qr), rmul((R)tab[3 + c], qi));
     for (int a = 0; a < iz.n; ++a)
       for (int b = 0; b < iy.n; ++b)
         for (int e = 0; e < ix.n; ++e) {
-          const long long cell = (long long)(iz.v[a] + 3) * g.ps + (long long)(iy.v[b] + 3) * g.px + g.xoff + ix.v[e];
+          const long long cell =
+              (long long)(iz.v[a] + 3) * g.ps + (long long)(iy.v[b] + 3) * g.px + g.xoff + ix.v[e];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) add_u<LAYOUT, R>(f, c * g.fs + cell, fc[c]);
+          for (int c = 0; c < 3; ++c) add_field<LAYOUT, R>(f, g, target, c, cell, fc[c]);
         }
   }
 }

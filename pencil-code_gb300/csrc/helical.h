@@ -27,11 +27,13 @@ struct HelGeom {
   int nx, ny, nz, px, my, xoff;
   long long ps, fs;   // plane and slice strides in elements
   double x0, y0, z0, dx, dy, dz, k1;
+  int iax;            // first slice of aa (field-major layouts)
+  int magnetic;       // 1: the force goes into aa (lmagnetic_forcing), 0: into uu
 };
 
 // Tables of the completed step (record ring[(nsub/3 - 1) % kHelRing], dt_last
-// of `state`) into `tab`, then uu += Re[(coef1 + i coef2) fx fy fz] on every
-// interior cell and its periodic ghost images.
+// of `state`) into `tab`, then the forced field += Re[(coef1 + i coef2) fx fy fz]
+// on every interior cell and its periodic ghost images.
 cudaError_t launch_helical(int layout, void* f, const HelRec* ring, const PcgbBoxState* state, double* tab,
                            const HelGeom& g, cudaStream_t s);
 

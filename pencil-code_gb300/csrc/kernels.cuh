@@ -49,9 +49,31 @@ KernelHandle kernel_f64_7(int tile);
 KernelHandle kernel_f64_8(int tile);
 KernelHandle kernel_dd_7(int tile);
 KernelHandle kernel_dd_8(int tile);
+// Variants with the upwind corrections, defined in kernels_upw_<type>.cu for the
+// tiles upw_tile() names (an empty handle for the others).
+KernelHandle kernel_f32_7_upw(int tile);
+KernelHandle kernel_f32_8_upw(int tile);
+KernelHandle kernel_f64_7_upw(int tile);
+KernelHandle kernel_f64_8_upw(int tile);
+KernelHandle kernel_dd_7_upw(int tile);
+KernelHandle kernel_dd_8_upw(int tile);
+
+// Tiles compiled with upwinding: the default tiles of the box and server
+// paths for each element type, and the field-major (32,8) FP32 tile.
+inline bool upw_tile(int dtype_bytes, int tile, int dfl = 0) {
+  if (dtype_bytes == 4) return tile == 1 || tile == 5 || tile == 6;
+  if (dfl) return tile == 2 || tile == 3 || tile == 5 || tile == 6;
+  return tile == 1 || tile == 2 || tile == 3;
+}
 
 // dfl: FP64-class state held as double-float pairs (8-byte elements, same tiles as FP64)
-inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile, int dfl = 0) {
+// upw: the variant with the upwind corrections
+inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile, int dfl = 0, bool upw = false) {
+  if (upw) {
+    if (dtype_bytes == 4) return nf == 8 ? kernel_f32_8_upw(tile) : kernel_f32_7_upw(tile);
+    if (dfl) return nf == 8 ? kernel_dd_8_upw(tile) : kernel_dd_7_upw(tile);
+    return nf == 8 ? kernel_f64_8_upw(tile) : kernel_f64_7_upw(tile);
+  }
   if (dtype_bytes == 4) return nf == 8 ? kernel_f32_8(tile) : kernel_f32_7(tile);
   if (dfl) return nf == 8 ? kernel_dd_8(tile) : kernel_dd_7(tile);
   return nf == 8 ? kernel_f64_8(tile) : kernel_f64_7(tile);
@@ -61,9 +83,9 @@ template <class CELL, int TX, int TY, int R, int MB>
 static KernelHandle make_kernel_handle();
 
 // Pair tiles of the double-float family (no kernel for the other element types).
-template <typename T, int NF, int TX, int TY>
+template <typename T, int NF, int TX, int TY, bool UPW = false>
 static KernelHandle make_dd_pair_handle() {
-  if constexpr (is_dd<T>::value) return make_kernel_handle<DDPairCell<NF, TX, TY>, TX, TY, 8, 1>();
+  if constexpr (is_dd<T>::value) return make_kernel_handle<DDPairCell<NF, TX, TY, UPW>, TX, TY, 8, 1>();
   else return KernelHandle();
 }
 
@@ -112,6 +134,38 @@ static KernelHandle make_kernel_handle() {
           case 1: cache[1] = make_kernel_handle<ScalarCell<T, NF, 16, 8>, 16, 8, 8, 1>(); break;   \
           case 2: cache[2] = make_kernel_handle<ScalarCell<T, NF, 24, 8>, 24, 8, 8, 1>(); break;   \
           default: cache[3] = make_kernel_handle<ScalarCell<T, NF, 32, 6>, 32, 6, 8, 1>(); break;  \
+        }                                                                                          \
+      }                                                                                            \
+      init[tile] = true;                                                                           \
+    }                                                                                              \
+    return cache[tile];                                                                            \
+  }                                                                                                \
+  }
+
+// Upwinding variants of the tiles upw_tile() names, same shapes, rings and
+// residency as the plain ones.
+#define PCGB_DEFINE_UPW_KERNELS(NAME, T, NF)                                                       \
+  namespace pcgb {                                                                                 \
+  KernelHandle NAME(int tile) {                                                                    \
+    static KernelHandle cache[kNumTiles];                                                          \
+    static bool init[kNumTiles] = {false, false, false, false, false, false, false, false};        \
+    if (tile < 0 || tile >= num_tiles(sizeof(T), is_dd<T>::value) ||                               \
+        !upw_tile(sizeof(T), tile, is_dd<T>::value))                                               \
+      return KernelHandle();                                                                       \
+    if (!init[tile]) {                                                                             \
+      if constexpr (sizeof(T) == 4) {                                                              \
+        switch (tile) {                                                                            \
+          case 1: cache[1] = make_kernel_handle<ScalarCell<T, NF, 32, 8, true>, 32, 8, 9, 1>(); break; \
+          case 5: cache[5] = make_kernel_handle<PairCell<NF, 32, 8, true>, 32, 8, 9, 1>(); break;  \
+          default: cache[6] = make_kernel_handle<PairCell<NF, 16, 8, true>, 16, 8, 8, 2>(); break; \
+        }                                                                                          \
+      } else {                                                                                     \
+        switch (tile) {                                                                            \
+          case 5: cache[5] = make_dd_pair_handle<T, NF, 16, 12, true>(); break;                    \
+          case 6: cache[6] = make_dd_pair_handle<T, NF, 16, 8, true>(); break;                     \
+          case 1: cache[1] = make_kernel_handle<ScalarCell<T, NF, 16, 8, true>, 16, 8, 8, 1>(); break; \
+          case 2: cache[2] = make_kernel_handle<ScalarCell<T, NF, 24, 8, true>, 24, 8, 8, 1>(); break; \
+          default: cache[3] = make_kernel_handle<ScalarCell<T, NF, 32, 6, true>, 32, 6, 8, 1>(); break; \
         }                                                                                          \
       }                                                                                            \
       init[tile] = true;                                                                           \

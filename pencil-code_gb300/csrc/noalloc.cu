@@ -99,12 +99,13 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
   const int xoff = 128 / tb;
   const int px = xoff + ((p->nx + 8 + xoff - 1) / xoff) * xoff;
   const int my = p->ny + 6, mz = p->nz + 6, mx = p->nx + 6;
-  const int tile = p->tile >= 0 ? p->tile : 0;
+  const bool upw = p->lupw_uu || p->lupw_lnrho;
+  const int tile = p->tile >= 0 ? p->tile : (upw ? 1 : 0);   // tile 1 has an upwinding variant in FP32 and FP64
   // the documented layout is field-major: only the field-major tile variants apply
   if (tile >= kNumScalarTiles) return fail(2, "tile variant out of range");
   const TileShape ts = tile_shape(tb, tile);
-  const KernelHandle kh = get_kernel(tb, nf, tile);
-  if (!kh.fn) return fail(2, "no kernel for this tile variant");
+  const KernelHandle kh = get_kernel(tb, nf, tile, 0, upw);
+  if (!kh.fn) return fail(2, upw ? "no upwinding kernel for this tile variant" : "no kernel for this tile variant");
   int zd = p->zdepth > 0 ? std::min(p->zdepth, p->nz) : p->nz;
 
   PcgbBoxDev h;
@@ -142,6 +143,7 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
   h.comp = 0;   // the FP32 carry would need state across calls; plain 2N update here
   h.diag_every = reductions ? 1 : 0;
   h.isothermal = (!p->lentropy && h.gamma_m1 == 0.0) ? 1 : 0;
+  h.lupw = (p->lupw_uu ? UPW_UU : 0) | (p->lupw_lnrho ? UPW_LNRHO : 0);
 
   cuuint64_t dims[4] = {(cuuint64_t)px, (cuuint64_t)my, (cuuint64_t)mz, (cuuint64_t)nf};
   cuuint64_t strides[3] = {(cuuint64_t)px * tb, (cuuint64_t)h.ps * tb, (cuuint64_t)h.fs * tb};

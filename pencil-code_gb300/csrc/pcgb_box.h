@@ -60,6 +60,7 @@ struct alignas(128) PcgbBoxDev {
   int comp;              // FP32 compensated 2N accumulation
   int diag_every;        // diagnostics at steps with step % diag_every == 0 (0: never)
   int isothermal;        // gamma == 1 without entropy
+  int lupw;              // upwinding of u.grad u / u.grad lnrho (UPW_* bits)
 };
 
 struct alignas(64) PcgbBoxState {

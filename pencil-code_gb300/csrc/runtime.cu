@@ -190,6 +190,7 @@ static void fill_physics(pcgb_box* b) {
   d.comp = (b->tb == 4 && p.comp) ? 1 : 0;
   d.diag_every = p.diag_every;
   d.isothermal = (!p.lentropy && d.gamma_m1 == 0.0) ? 1 : 0;
+  d.lupw = (p.lupw_uu ? UPW_UU : 0) | (p.lupw_lnrho ? UPW_LNRHO : 0);
 }
 
 // ABC forcing tables sin/cos(kf*x) over the ghosted grid, forcing.f90:1100-1104,
@@ -265,7 +266,9 @@ static int set_tiling(pcgb_box* b, int tile, int zd) {
   if ((int)tile_is_pair(b->tb, tile, b->dfl) != b->pairs)
     return set_err(PCGB_E_ARG, "tile %d needs a different device layout than this box was created with", tile);
   TileShape ts = tile_shape(b->tb, tile, b->dfl);
-  KernelHandle kh = get_kernel(b->tb, b->nf, tile, b->dfl);
+  const bool upw = b->hdev.lupw != 0;
+  KernelHandle kh = get_kernel(b->tb, b->nf, tile, b->dfl, upw);
+  if (!kh.fn && upw) return set_err(PCGB_E_UNSUPPORTED, "tile %d has no upwinding variant", tile);
   if (!kh.fn) return set_err(PCGB_E_ARG, "no kernel for tile %d", tile);
   if (kh.smem > g.max_smem) return set_err(PCGB_E_UNSUPPORTED, "tile %d needs %d B shared memory", tile, kh.smem);
   b->tile = tile; b->tx = ts.tx; b->ty = ts.ty; b->kh = kh;
@@ -311,6 +314,11 @@ static int validate(const pcgb_params* p) {
   if (p->dt < 0) return set_err(PCGB_E_ARG, "dt must be >= 0");
   if (p->lforcing_hel != 0 && p->lforcing_hel != 1) return set_err(PCGB_E_ARG, "lforcing_hel must be 0 or 1");
   if (p->lforcing_hel && !(p->force_hel >= 0.0)) return set_err(PCGB_E_ARG, "force_hel must be >= 0");
+  if (p->lmagnetic_forcing != 0 && p->lmagnetic_forcing != 1) return set_err(PCGB_E_ARG, "lmagnetic_forcing must be 0 or 1");
+  if (p->lmagnetic_forcing && !p->lforcing_hel)
+    return set_err(PCGB_E_ARG, "lmagnetic_forcing applies to random helical forcing (lforcing_hel)");
+  if ((p->lupw_uu != 0 && p->lupw_uu != 1) || (p->lupw_lnrho != 0 && p->lupw_lnrho != 1))
+    return set_err(PCGB_E_ARG, "lupw_uu and lupw_lnrho must be 0 or 1");
   return 0;
 }
 
@@ -605,17 +613,22 @@ static int hel_layout(const pcgb_box* b) {
 }
 
 // Random helical forcing of the step that starts now: draw its record into the
-// device ring (forcing.f90 fconst_coefs_hel), applied when the step ends.
+// device ring (forcing.f90 fconst_coefs_hel), applied when the step ends.  With
+// magnetic forcing the step also draws the secondary record of lmhd_forcing
+// (forcing_hel, forcing.f90:2136-2141), whose force on uu is zero by default,
+// so the stream advances as the reference's does.
 static int helical_begin_step(pcgb_box* b) {
   if (b->kvec.empty()) return set_err(PCGB_E_STATE, "helical forcing needs wavevectors (pcgb_box_set_kvectors)");
-  HelRec rec;
+  HelRec rec, secondary;
   const int nk = (int)(b->kvec.size() / 3);
   helical_record(b->p.cs0, b->p.relhel, b->p.force_hel, b->kvec.data(), nk, b->kav, &b->rng, &rec);
+  if (b->p.lmagnetic_forcing)
+    helical_record(b->p.cs0, b->p.relhel, b->p.force_hel, b->kvec.data(), nk, b->kav, &b->rng, &secondary);
   CK(cudaMemcpyAsync(b->dring + (b->nsub / 3) % kHelRing, &rec, sizeof(rec), cudaMemcpyHostToDevice, g.stream));
   return 0;
 }
 
-// addforce (forcing.f90:1307) after the step: uu of the new state += the force.
+// addforce (forcing.f90:1307) after the step: uu (aa with magnetic forcing) of the new state += the force.
 static int helical_end_step(pcgb_box* b) {
   const pcgb_params& p = b->p;
   HelGeom hg;
@@ -624,6 +637,8 @@ static int helical_end_step(pcgb_box* b) {
   hg.x0 = p.xyz0[0]; hg.y0 = p.xyz0[1]; hg.z0 = p.xyz0[2];
   hg.dx = p.Lxyz[0] / p.nx; hg.dy = p.Lxyz[1] / p.ny; hg.dz = p.Lxyz[2] / p.nz;
   hg.k1 = p.kf;
+  hg.iax = b->nf - 3;
+  hg.magnetic = p.lmagnetic_forcing ? 1 : 0;
   CK(launch_helical(hel_layout(b), b->f[cur_in(b)], b->dring, b->dstate, b->dtab, hg, g.stream));
   g.launches += 2;
   return 0;
@@ -738,8 +753,8 @@ extern "C" pcgb_batch* pcgb_batch_create(pcgb_box** boxes, int n, int persistent
   B->boxes.assign(boxes, boxes + n);
   for (auto* b : B->boxes) {
     if (!b || b->tb != boxes[0]->tb || b->dfl != boxes[0]->dfl || b->nf != boxes[0]->nf ||
-        b->tile != boxes[0]->tile) {
-      set_err(PCGB_E_ARG, "a batch needs boxes of one class (precision, fields, tile)");
+        b->tile != boxes[0]->tile || b->kh.fn != boxes[0]->kh.fn) {
+      set_err(PCGB_E_ARG, "a batch needs boxes of one class (precision, fields, tile, upwinding)");
       delete B;
       return nullptr;
     }
@@ -871,7 +886,7 @@ extern "C" int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, doubl
   if (!b) { cudaEventDestroy(e0); cudaEventDestroy(e1); return g_err; }
   if (bt < 0) { bt = b->tile; bz = b->zd; }
   for (int t = fam * kNumScalarTiles; t < (fam + 1) * kNumScalarTiles && t < ntile; ++t) {
-    KernelHandle kh = get_kernel(b->tb, b->nf, t, b->dfl);
+    KernelHandle kh = get_kernel(b->tb, b->nf, t, b->dfl, b->hdev.lupw != 0);
     if (!kh.fn || kh.smem > g.max_smem) continue;
     std::vector<int> zs = {b->nz, 256, 128, 64, 32, 16};
     std::sort(zs.begin(), zs.end());
@@ -1042,10 +1057,12 @@ static int box_reload(pcgb_box* b, const pcgb_params& p) {
   if (p.nx != b->p.nx || p.ny != b->p.ny || p.nz != b->p.nz || p.lentropy != b->p.lentropy ||
       p.precision != b->p.precision || p.dfloat != b->p.dfloat)
     return set_err(PCGB_E_ARG, "reloadConfig cannot change grid, field count or precision");
+  const int upw_was = b->hdev.lupw;
   b->p = p;
   fill_physics(b);
   int rc = upload_forcing(b);
   if (rc) return rc;
+  if ((b->hdev.lupw != 0) != (upw_was != 0) && (rc = set_tiling(b, b->tile, b->zd))) return rc;   // kernel variant
   CK(cudaMemcpyAsync(b->ddev, &b->hdev, sizeof(PcgbBoxDev), cudaMemcpyHostToDevice, g.stream));
   if (p.dt > 0) return pcgb_box_set_dt(b, p.dt);
   CK(cudaStreamSynchronize(g.stream));

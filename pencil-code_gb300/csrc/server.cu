@@ -58,7 +58,7 @@ struct pcgb_server {
   std::deque<Req*> queue;
   std::vector<Req*> active;
   std::map<long long, Req*> all;
-  std::map<int, ClassBatch> batches;   // key: (dfloat*16 + precision)*16 + nf
+  std::map<int, ClassBatch> batches;   // key: ((upwinding*2 + dfloat)*16 + precision)*16 + nf
   std::thread th;
   bool stop = false;
   size_t used = 0, peak_bytes = 0;
@@ -149,7 +149,10 @@ void pcgb_server::run() {
     if (steps < 1) steps = 1;
     // one batch per class; rebuilt when its membership changed
     std::map<int, std::vector<pcgb_box*>> cls;
-    for (Req* r : act) cls[(r->p.dfloat * 16 + r->p.precision) * 16 + (r->p.lentropy ? 8 : 7)].push_back(r->box);
+    for (Req* r : act) {
+      const int upw = (r->p.lupw_uu || r->p.lupw_lnrho) ? 1 : 0;   // the upwinding kernel variant is its own class
+      cls[((upw * 2 + r->p.dfloat) * 16 + r->p.precision) * 16 + (r->p.lentropy ? 8 : 7)].push_back(r->box);
+    }
     bool ok = true;
     for (auto& kv : cls) {
       ClassBatch& cb = batches[kv.first];

@@ -37,6 +37,7 @@ class Params(C.Structure):
         ("dt", C.c_double), ("dt_mode", C.c_int), ("diag_every", C.c_int),
         ("tile", C.c_int), ("zdepth", C.c_int), ("dfloat", C.c_int),
         ("lforcing_hel", C.c_int), ("seed_ff", C.c_int), ("force_hel", C.c_double),
+        ("lupw_uu", C.c_int), ("lupw_lnrho", C.c_int), ("lmagnetic_forcing", C.c_int), ("pad_", C.c_int),
     ]
 
     def update(self, **kw) -> "Params":

@@ -9,9 +9,11 @@ src/param_io.f90:82-250, :461-570, restricted to the keys of this hot path:
   &viscosity_run_pars   nu, ivisc ('nu-const' only)
   &magnetic_run_pars    eta, b_ext (B_ext), iresistivity ('eta-const' only)
   &entropy_run_pars     chi, iheatcond ('chi-const' only), lviscosity_heat
-  &hydro_run_pars       lforcing_cont_uu, ampl_fcont_uu
+  &hydro_run_pars       lforcing_cont_uu, ampl_fcont_uu, lupw_uu
+  &density_run_pars     lupw_lnrho
   &forcing_run_pars     lforcing_cont, iforcing_cont ('ABC'), ampl_ff, k1_ff, kf_fcont, relhel,
-                        ABC_A, ABC_B, ABC_C; iforce ('helical' or 'zero'), force
+                        ABC_A, ABC_B, ABC_C; iforce ('helical' or 'zero'), force,
+                        lmagnetic_forcing (with lhydro_forcing=T, crosshel=0)
   &magnetic_init_pars   initaa, amplaa (initial condition, returned separately)
 
 Keys outside this set are kept in ``extra`` so a caller can see what was not applied.
@@ -144,6 +146,8 @@ def params_from_namelists(start_text: str, run_text: str, n=(32, 32, 32), lentro
     take("entropy_run_pars", "chi", lambda v: setattr(p, "chi", float(_first(v))))
     take("entropy_run_pars", "lviscosity_heat", lambda v: setattr(p, "lviscosity_heat", int(bool(v))))
     take("hydro_run_pars", "ampl_fcont_uu", lambda v: setattr(p, "ampl_fcont_uu", float(_first(v))))
+    take("hydro_run_pars", "lupw_uu", lambda v: setattr(p, "lupw_uu", int(bool(v))))
+    take("density_run_pars", "lupw_lnrho", lambda v: setattr(p, "lupw_lnrho", int(bool(v))))
     fr = g.get("forcing_run_pars", {})
     hr = g.get("hydro_run_pars", {})
     cont = bool(fr.get("lforcing_cont", False)) and bool(hr.get("lforcing_cont_uu", False))
@@ -163,13 +167,24 @@ def params_from_namelists(start_text: str, run_text: str, n=(32, 32, 32), lentro
     take("forcing_run_pars", "abc_a", lambda v: setattr(p, "abc_a", float(_first(v))))
     take("forcing_run_pars", "abc_b", lambda v: setattr(p, "abc_b", float(_first(v))))
     take("forcing_run_pars", "abc_c", lambda v: setattr(p, "abc_c", float(_first(v))))
+    take("forcing_run_pars", "lmagnetic_forcing", lambda v: setattr(p, "lmagnetic_forcing", int(bool(v))))
+    if p.lmagnetic_forcing and not p.lforcing_hel:
+        raise ValueError("lmagnetic_forcing is implemented for iforce='helical' only")
+    # forcing of the vector potential as forcing_hel does it with the defaults
+    # lhydro_forcing=T, crosshel=0, lforcing2_same=F, lforcing2_curl=F
+    for key, default in (("lhydro_forcing", True), ("crosshel", 0.0), ("lforcing2_same", False),
+                         ("lforcing2_curl", False)):
+        if key in fr and _first(fr[key]) != default:
+            raise ValueError(f"{key}={_first(fr[key])!r}: only the default {default!r} is implemented")
     known = {"run_pars": {"dt", "nt", "cdt", "cdtv", "itorder", "it1", "lbidiagonal_derij", "cvsid", "isave",
                           "dsnap", "dvid", "dspec", "ou_spec", "ab_spec", "lpencil_check"},
              "viscosity_run_pars": {"nu", "ivisc"}, "magnetic_run_pars": {"eta", "b_ext", "iresistivity"},
              "entropy_run_pars": {"chi", "iheatcond", "lviscosity_heat"},
-             "hydro_run_pars": {"lforcing_cont_uu", "ampl_fcont_uu"},
+             "hydro_run_pars": {"lforcing_cont_uu", "ampl_fcont_uu", "lupw_uu"},
+             "density_run_pars": {"lupw_lnrho"},
              "forcing_run_pars": {"lforcing_cont", "iforcing_cont", "ampl_ff", "k1_ff", "kf_fcont", "relhel",
-                                  "abc_a", "abc_b", "abc_c", "iforce", "force"}}
+                                  "abc_a", "abc_b", "abc_c", "iforce", "force", "lmagnetic_forcing",
+                                  "lhydro_forcing", "crosshel", "lforcing2_same", "lforcing2_curl"}}
     for grp, keys in known.items():
         for k, v in g.get(grp, {}).items():
             if re.sub(r"\(.*\)$", "", k) not in keys:
@@ -191,3 +206,21 @@ def read_kdat(path: str):
         vals = fh.read().split()
     nk, kav = int(vals[0]), float(vals[1])
     return np.array([float(v) for v in vals[2:2 + 3 * nk]]).reshape(3, nk), kav
+
+
+def kvector_shell(k2min: int, k2max: int):
+    """The integer wavevectors with k2min <= |k|^2 <= k2max, in the order the
+    reference's k.dat files list them (kx, then ky, then kz ascending), and their
+    mean |k| (kav).  The forcing shells of the reference's samples are of this
+    form: |k|^2 in [8, 12] is samples/helical-MHDturb/k.dat (98 vectors) and
+    [3577, 3624] the 17550 vectors of its 4096^3 timing run."""
+    import numpy as np
+    kmax = int(np.floor(np.sqrt(k2max)))
+    g = np.arange(-kmax, kmax + 1)
+    kx, ky, kz = np.meshgrid(g, g, g, indexing="ij")
+    k2 = kx * kx + ky * ky + kz * kz
+    sel = (k2 >= k2min) & (k2 <= k2max)
+    kvec = np.stack([kx[sel], ky[sel], kz[sel]]).astype(np.float64)
+    if kvec.shape[1] == 0:
+        raise ValueError(f"no integer wavevector with {k2min} <= |k|^2 <= {k2max}")
+    return kvec, float(np.sqrt(k2[sel]).mean())

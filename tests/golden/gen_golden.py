@@ -23,7 +23,13 @@ nowhere else):
 4. var_subrecords.json -- a small snapshot written by
    pencil-code_gb300/vardat.py with a tiny subrecord size, checked at
    generation time to read back identically through FortranFileExt.
+6. timings_n4096_ref.json -- doc/timings/N4096_32x32x32, the reference's
+   timing configuration (upwinded advection, helical forcing of the vector
+   potential): its start.in / run.in text, its time series, and its k.dat
+   summarised as count, kav, the |k|^2 range and a SHA-256 of the vectors
+   (int16, shape (3, nk)), so a regenerated shell can be checked against it.
 """
+import hashlib
 import importlib.util
 import json
 import os
@@ -169,6 +175,36 @@ def main(ref_root):
     with open(os.path.join(here, "helical_mhdturb_ref.json"), "w") as fh:
         json.dump({"params": hpar, "kdat": {"nk": nk, "kav": kav, "kxyz": kk}, "series": series,
                    "namelists": hnl}, fh, indent=1)
+
+    # the timing configuration of doc/timings (namelists, time series, k.dat digest)
+    tdir = os.path.join(ref_root, "doc", "timings", "N4096_32x32x32")
+    with open(os.path.join(tdir, "k.dat")) as fh:
+        vals = fh.read().split()
+    tnk, tkav = int(vals[0]), float(vals[1])
+    tk = np.array([int(float(v)) for v in vals[2:2 + 3 * tnk]], dtype=np.int16).reshape(3, tnk)
+    tk2 = (tk.astype(np.int64) ** 2).sum(0)
+    tnl = {}
+    for name in ("start.in", "run.in", "print.in"):
+        with open(os.path.join(tdir, name)) as fh:
+            tnl[name] = fh.read()
+    tseries = []
+    with open(os.path.join(tdir, "data", "time_series.dat")) as fh:
+        cols = None
+        for line in fh:
+            if line.startswith("#"):
+                cols = [c for c in line.strip("#\n").replace("-", " ").split()]
+                continue
+            v = line.split()
+            tseries.append({c: (int(x) if c == "it" else float(x)) for c, x in zip(cols, v)})
+    with open(os.path.join(tdir, "data", "dim.dat")) as fh:
+        tdim = fh.read().split()
+    with open(os.path.join(here, "timings_n4096_ref.json"), "w") as fh:
+        json.dump({"kdat": {"nk": tnk, "kav": tkav, "k2min": int(tk2.min()), "k2max": int(tk2.max()),
+                            "sha256_int16": hashlib.sha256(tk.astype("<i2").tobytes()).hexdigest()},
+                   "namelists": tnl, "series": tseries,
+                   "grid": {"nxgrid": 4096, "ncpus": 32768, "precision": tdim[6]},
+                   "source": "doc/timings/N4096_32x32x32/{start.in,run.in,print.in,k.dat,data/time_series.dat,"
+                             "data/dim.dat,src/cparam.local}"}, fh, indent=1)
 
     with open(os.path.join(here, "var_subrecords.json"), "w") as fh:
         json.dump({"dim": [mx, my, mz, nv], "seed": 7, "max_subrecord": 1000, "file_bytes": size,

@@ -5,6 +5,7 @@ a var.dat committed with a reference sample run together with what the
 reference's own record reader reads from it, and the MHD-ABCforcing sample's
 namelist files.
 """
+import hashlib
 import importlib
 import json
 import os
@@ -175,3 +176,41 @@ def test_namelists_of_helical_mhdturb_sample(tmp_path):
     assert kav == kd["kav"] and np.array_equal(k2, kk)
     with pytest.raises(ValueError, match="iforce"):
         nl.params_from_namelists("", "&forcing_run_pars iforce='irrotational' /")
+
+
+def test_kvector_shells_match_reference_kdat():
+    ref = _json("helical_mhdturb_ref.json")["kdat"]
+    kv, kav = nl.kvector_shell(8, 12)
+    assert kv.shape == (3, ref["nk"]) and np.array_equal(kv.ravel(), np.array(ref["kxyz"]))
+    assert float("%.6g" % kav) == ref["kav"]
+    t = _json("timings_n4096_ref.json")["kdat"]
+    kv, kav = nl.kvector_shell(t["k2min"], t["k2max"])
+    assert kv.shape == (3, t["nk"])
+    digest = hashlib.sha256(kv.astype("<i2").tobytes()).hexdigest()
+    assert digest == t["sha256_int16"]
+    assert abs(kav - t["kav"]) < 1e-3
+
+
+def test_namelists_of_timing_configuration():
+    """doc/timings/N4096_32x32x32: upwinded advection and density, helical forcing of aa."""
+    ref = _json("timings_n4096_ref.json")
+    p, ic, extra = nl.params_from_namelists(ref["namelists"]["start.in"], ref["namelists"]["run.in"],
+                                            n=(64, 64, 64), precision=4)
+    assert p.lupw_uu == 1 and p.lupw_lnrho == 1
+    assert p.lforcing_hel == 1 and p.lmagnetic_forcing == 1 and p.force_hel == 5e-4 and p.relhel == 1.0
+    assert p.nu == 2e-5 and p.eta == 2e-5 and p.cdt == 0.9 and p.gamma == 1.0 and p.dt == 0.0
+    assert ic["nt"] == 200 and ic["it1"] == 50 and ic["dsnap"] == 2.0
+    # output-only switches are reported as not applied
+    assert "magnetic_run_pars.lbb_as_aux" in extra and "run_pars.downsampl" in extra
+    # its time series: the velocity is not forced, brms grows
+    s = {r["it"]: r for r in ref["series"]}
+    assert s[150]["urms"] == 0.0 and s[150]["brms"] > s[50]["brms"] > 0.0
+
+
+def test_magnetic_forcing_options_are_checked():
+    with pytest.raises(ValueError, match="lmagnetic_forcing"):
+        nl.params_from_namelists("", "&forcing_run_pars lmagnetic_forcing=T /")
+    with pytest.raises(ValueError, match="crosshel"):
+        nl.params_from_namelists("", "&forcing_run_pars iforce='helical', lmagnetic_forcing=T, crosshel=1. /")
+    with pytest.raises(ValueError, match="lhydro_forcing"):
+        nl.params_from_namelists("", "&forcing_run_pars iforce='helical', lhydro_forcing=F /")
