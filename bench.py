@@ -18,6 +18,13 @@ dt=2e-4.  A step is one full RK3 step (3 substep kernel launches).
   cpu_baseline  the FP64 oracle (C restatement of the reference Fortran) on
              all host cores over a bounded sample.
 
+--workload timings runs the physics of the reference's own timing run
+(doc/timings/N4096_32x32x32: isothermal MHD, upwinded u.grad u and
+u.grad lnrho, random helical forcing of the vector potential at |k| = 60 with
+force 5e-4, nu = eta = 2e-5, CFL dt with cdt = 0.9 from the current state),
+single precision as that run was, zero initial fields, on an n^3 box (1024^3
+by default); its us_per_pt_step is the reference's timing unit.
+
 --impl reference runs that CPU implementation alone on the same metric.
 Under torchrun with N>1 every rank advances its own replica (weak scaling).
 """
@@ -122,6 +129,32 @@ def headline_params(pc, n: int, precision: int, lentropy: int = 0, dfloat: int =
     return p
 
 
+# doc/timings/N4096_32x32x32: k.dat is the shell 3577 <= |k|^2 <= 3624 (17550
+# vectors) with kav = 60.0044 as that file gives it
+TIMINGS_K2 = (3577, 3624)
+TIMINGS_KAV = 60.0044
+# the reference's published times per point and step for 1024^3 and 2048^3
+# (doc/manual.tex:9527, :9537), single precision, Triolith
+TIMINGS_PUBLISHED = [
+    {"us_per_pt_step": 3.6e-4, "grid": 1024, "procs": 4096, "system": "Triolith", "source": "doc/manual.tex:9527"},
+    {"us_per_pt_step": 1.475e-4, "grid": 2048, "procs": 8192, "system": "Triolith (kf=60 run)",
+     "source": "doc/manual.tex:9537"},
+]
+
+
+def timings_params(pc, n: int, precision: int = 4):
+    """The run parameters of doc/timings/N4096_32x32x32 (start.in, run.in) on an n^3 box."""
+    return pc.default_params(nx=n, ny=n, nz=n, precision=precision, comp=1, gamma=1.0, nu=2e-5, eta=2e-5,
+                             cdt=0.9, dt=0.0, dt_mode=2, lupw_uu=1, lupw_lnrho=1, lforcing_hel=1, force_hel=5e-4,
+                             relhel=1.0, lmagnetic_forcing=1, seed_ff=1812)
+
+
+def timings_kvectors():
+    nl = importlib.import_module("pencil-code_gb300.namelist")
+    kvec, _ = nl.kvector_shell(*TIMINGS_K2)
+    return np.ascontiguousarray(kvec), TIMINGS_KAV
+
+
 def init_headline(box, p):
     iax = 5 if p.lentropy else 4
     for k in range(iax):
@@ -144,23 +177,44 @@ def time_box_steps(pc, torch, box, stream, steps: int) -> tuple[float, int]:
     return e0.elapsed_time(e1), int(L.pcgb_launch_count() - n0)
 
 
-def cpu_oracle_rate(n: int, steps: int, threads: int, lentropy: int = 0) -> tuple[float, float, dict]:
-    """Gcell-updates/s per substep of the FP64 oracle on an n^3 sample of the headline physics."""
+def cpu_oracle_rate(n: int, steps: int, threads: int, lentropy: int = 0,
+                    workload: str = "headline") -> tuple[float, float, dict]:
+    """Gcell-updates/s per substep of the FP64 oracle on an n^3 sample of the workload's physics."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
-    op = O.make_params(nx=n, ny=n, nz=n, lentropy=lentropy, gamma=1.0 if not lentropy else 5.0 / 3.0,
-                       nu=5e-4, eta=5e-4, chi=5e-4 if lentropy else 0.0, lforcing_cont=1, ampl_ff=0.02, kf=2.0)
+    timings = workload == "timings"
+    if timings:
+        op = O.make_params(nx=n, ny=n, nz=n, gamma=1.0, nu=2e-5, eta=2e-5, cdt=0.9, lupw_uu=1, lupw_lnrho=1)
+    else:
+        op = O.make_params(nx=n, ny=n, nz=n, lentropy=lentropy, gamma=1.0 if not lentropy else 5.0 / 3.0,
+                           nu=5e-4, eta=5e-4, chi=5e-4 if lentropy else 0.0, lforcing_cont=1, ampl_ff=0.02,
+                           kf=2.0)
     f = O.empty_f(op)
     df = O.empty_f(op)
     rng = np.random.Generator(np.random.PCG64(1))
     iax = 5 if lentropy else 4
     f[3:-3, 3:-3, 3:-3, iax:iax + 3] = 1e-5 * rng.standard_normal((n, n, n, 3))
+    kvec, kav = timings_kvectors() if timings else (None, None)
+    state = 1812
+
+    def step(t, dt):
+        nonlocal state
+        if not timings:
+            t, dt, _ = O.time_step(op, f, df, t, dt, False, nthreads=threads)
+            return t, dt
+        rec, state = O.helical_coefs(op, 5e-4, kvec, kav, state)
+        _, state = O.helical_coefs(op, 5e-4, kvec, kav, state)   # secondary record of lmhd_forcing
+        t, dt, _ = O.time_step(op, f, df, t, 0.0, True, nthreads=threads)
+        O.add_helical(op, f, rec, dt, 1)
+        O.ghosts(op, f)
+        return t, dt
+
     t, dt = 0.0, 2e-4
-    O.time_step(op, f, df, t, dt, False, nthreads=threads)   # warm-up (page-in, thread spin-up)
+    t, dt = step(t, dt)   # warm-up (page-in, thread spin-up)
     t0 = time.perf_counter()
     for _ in range(steps):
-        t, dt, _ = O.time_step(op, f, df, t, dt, False, nthreads=threads)
+        t, dt = step(t, dt)
     el = time.perf_counter() - t0
     return n ** 3 * 3 * steps / el / 1e9, el, {"n": n, "steps": steps}
 
@@ -196,7 +250,7 @@ def run_reference(args):
     n = args.cpu_sample_n
     per = []
     for i in range(args.warmup + args.steps):
-        rate, el, _ = cpu_oracle_rate(n, 1, threads)
+        rate, el, _ = cpu_oracle_rate(n, 1, threads, workload=args.workload)
         if i >= args.warmup:
             per.append((rate, el))
     total_cells = n ** 3 * 3 * len(per)
@@ -207,7 +261,9 @@ def run_reference(args):
         "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total_t / len(per), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"isothermal MHD {args.n}^3 headline physics, CPU sample {n}^3 per step",
+        "config": {"workload": f"isothermal MHD {args.n}^3 "
+                               f"{'timing-run' if args.workload == 'timings' else 'headline'} physics, "
+                               f"CPU sample {n}^3 per step",
                    "sample_n": n},
         "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
                          "sample": f"{n}^3 box, 1 RK3 step per timed step, FP64 oracle, OpenMP {threads} threads"},
@@ -231,14 +287,24 @@ def run_ours(args):
     L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
 
     n, prec = args.n, args.precision
-    p = headline_params(pc, n, prec, args.lentropy, args.dfloat)
+    timings = args.workload == "timings"
+    if timings:
+        p = timings_params(pc, n, prec)
+        kvec, kav = timings_kvectors()
+    else:
+        p = headline_params(pc, n, prec, args.lentropy, args.dfloat)
     if args.tile >= 0:
         p.tile = args.tile
     if args.zdepth > 0:
         p.zdepth = args.zdepth
     nf = 8 if args.lentropy else 7
     box = pc.Box(p)
-    init_headline(box, p)
+    if timings:
+        box.set_kvectors(kvec, kav)
+        for k in range(nf):
+            box.init_field(k, "zero")   # the timing run starts from zero fields (start.in)
+    else:
+        init_headline(box, p)
     info = box.info()
     box.steps(args.warmup)
     box.sync()
@@ -253,7 +319,10 @@ def run_ours(args):
     ms = max_over_ranks(ms, device="cuda")
     cells = float(n) ** 3
     value = whole_job_value(cells, args.steps, ws, ms)
-    per_launch_ms = ms / launches if launches else float("nan")
+    # time per substep kernel: with the headline physics every launch is a substep;
+    # the timing-run physics adds a CFL pass and the two forcing kernels per step,
+    # charged here to the substeps (a lower bound on the substep kernel's rate)
+    per_launch_ms = ms / (3 * args.steps)
     bpc = bytes_per_cell_substep(nf, prec, True)
     achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
@@ -273,13 +342,16 @@ def run_ours(args):
     # ---- e2e through the plug-in C ABI with pinned host buffers ----
     e2e = None
     if not args.no_e2e:
+        if timings:
+            L.pcgb_set_kvectors(kvec.ctypes.data_as(C.POINTER(C.c_double)), kvec.shape[1], kav)
         e2e = run_e2e(args, pc, gpu, torch, stream, p, nf, ws)
 
     # ---- CPU baseline (rank 0, N=1 only) ----
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, el, smp = cpu_oracle_rate(args.cpu_sample_n, args.cpu_sample_steps, threads, args.lentropy)
+        rate, el, smp = cpu_oracle_rate(args.cpu_sample_n, args.cpu_sample_steps, threads, args.lentropy,
+                                        args.workload)
         cpu = {"value": rate, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
                "sample": f"{smp['n']}^3 box, {smp['steps']} RK3 steps of the same physics, FP64 oracle "
                          f"(C restatement of the reference Fortran), OpenMP {threads} threads, {el:.1f} s"}
@@ -293,10 +365,14 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if prec == 4 else ("f32x2 (double-float)" if args.dfloat else "f64"),
             "data": "synthetic (seeded on device)",
-            "config": {"workload": f"{'entropy' if args.lentropy else 'isothermal'} MHD {n}^3, {nf} fields, "
-                                   f"{'FP32 compensated' if prec == 4 else ('FP64-class double-float' if args.dfloat else 'FP64')}"
-                                   f", nu=eta=5e-4, ABC k=2 ampl 0.02, "
-                                   f"dt=2e-4", "grid": n, "fields": nf,
+            "config": {"workload": (f"timing-run physics (doc/timings/N4096_32x32x32: lupw_uu, lupw_lnrho, "
+                                    f"helical forcing of aa at |k|=60, force 5e-4, nu=eta=2e-5, CFL dt cdt=0.9 "
+                                    f"from the current state) on {n}^3, 7 fields, "
+                                    f"{'FP32 compensated' if prec == 4 else 'FP64'}") if timings else
+                                   (f"{'entropy' if args.lentropy else 'isothermal'} MHD {n}^3, {nf} fields, "
+                                    f"{'FP32 compensated' if prec == 4 else ('FP64-class double-float' if args.dfloat else 'FP64')}"
+                                    f", nu=eta=5e-4, ABC k=2 ampl 0.02, "
+                                    f"dt=2e-4"), "grid": n, "fields": nf,
                        "tile": info["tile"], "zdepth": info["zdepth"],
                        "l2": "inputs larger than L2 (state %.1f GB)" % (3 * nf * cells * prec / 1e9),
                        "parallelism": f"replicas x{ws}"},
@@ -305,6 +381,8 @@ def run_ours(args):
                          "bytes_per_cell_substep": bpc},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
         }
+        if timings:
+            line["published_reference"] = TIMINGS_PUBLISHED
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -470,7 +548,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=96)
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
-    ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "serve"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "timings", "ensemble", "serve"])
     ap.add_argument("--boxes", type=int, default=192)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--graph-steps", type=int, default=10)

@@ -69,11 +69,14 @@ typedef struct pcgb_params {
                               after every step; wavevectors from pcgb_box_set_kvectors / pcgb_set_kvectors */
   int seed_ff;             /* seed of the forcing's random stream (ran0, general.f90:867) */
   double force_hel;        /* &forcing_run_pars force (amplitude of the helical forcing) */
-  int lupw_uu;             /* &hydro_run_pars lupw_uu: upwinded u.grad u (5th-order correction) */
-  int lupw_lnrho;          /* &density_run_pars lupw_lnrho: upwinded u.grad lnrho */
+  int lupw_uu;             /* &hydro_run_pars lupw_uu: u.grad u minus sum_j |u_j| D6_j u (hydro.f90:3662,
+                              sub.f90:7491); runs the upwinding kernel variant of the tile */
+  int lupw_lnrho;          /* &density_run_pars lupw_lnrho: the same correction of u.grad lnrho
+                              (density.f90:2772) */
   int lmagnetic_forcing;   /* &forcing_run_pars lmagnetic_forcing with iforce='helical': the force goes
-                              into aa and a second, independent force into uu (forcing.f90:314-340) */
-  int pad_;
+                              into aa; each step also draws the secondary record of lmhd_forcing, whose
+                              force on uu is zero for crosshel = 0 (forcing.f90:314-345, :2136-2311) */
+  int pad_;                /* keeps the struct a multiple of 8 bytes; set to 0 */
 } pcgb_params;
 
 /* Defaults of the reference (cdata.f90:211,235,239; eos_idealgas.f90:47;
