@@ -109,34 +109,66 @@ __device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
 
-// component c of uu (target 0) or aa (target 1) at cell `cell` += v
+// The interior cell (x, y, z) and its periodic ghost images, as element offsets.
+struct CellImages {
+  Images ix, iy, iz;
+  long long ps, px, xoff;
+  __device__ __forceinline__ CellImages(int i, int j, int k, const HelGeom& g)
+      : ix(i, g.nx), iy(j, g.ny), iz(k, g.nz), ps(g.ps), px(g.px), xoff(g.xoff) {}
+  __device__ __forceinline__ long long at(int a, int b, int e) const {
+    return (long long)(iz.v[a] + 3) * ps + (long long)(iy.v[b] + 3) * px + xoff + ix.v[e];
+  }
+  // store w at every image (the interior cell included)
+  template <typename E>
+  __device__ __forceinline__ void store(E* p, const E& w) const {
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+          if (a < iz.n && b < iy.n && e < ix.n) p[at(a, b, e)] = w;
+  }
+};
+
+// Component c of uu (target 0) or aa (target 1): the value at the interior
+// cell plus v, stored there and at the cell's periodic ghost images (copies of
+// the interior value after a substep).  Pair layouts move whole elements; only
+// the target lane changes.
 template <int LAYOUT, typename R>
-__device__ __forceinline__ void add_field(void* f, const HelGeom& g, int target, int c, long long cell, R v) {
+__device__ __forceinline__ void add_force(void* f, const HelGeom& g, int target, int c, const CellImages& ci, R v) {
+  const long long cell = ci.at(0, 0, 0);
   if (LAYOUT == HEL_F32 || LAYOUT == HEL_F64 || LAYOUT == HEL_DD) {
-    const long long e = (long long)(target ? g.iax + c : c) * g.fs + cell;   // field-major slice
+    const long long base = (long long)(target ? g.iax + c : c) * g.fs;   // field-major slice
     if (LAYOUT == HEL_F32) {
-      float* p = static_cast<float*>(f) + e;
-      *p = radd(*p, (float)v);
+      float* p = static_cast<float*>(f) + base;
+      ci.store(p, radd(p[cell], (float)v));
     } else if (LAYOUT == HEL_F64) {
-      double* p = static_cast<double*>(f) + e;
-      *p = radd(*p, (double)v);
+      double* p = static_cast<double*>(f) + base;
+      ci.store(p, radd(p[cell], (double)v));
     } else {
-      float* p = static_cast<float*>(f) + 2 * e;   // (hi, lo)
-      const dd w(__dadd_rn((double)p[0] + (double)p[1], (double)v));
-      p[0] = w.hi;
-      p[1] = w.lo;
+      float2* p = static_cast<float2*>(f) + base;   // (hi, lo)
+      const float2 e = p[cell];
+      const dd w(__dadd_rn((double)e.x + (double)e.y, (double)v));
+      ci.store(p, make_float2(w.hi, w.lo));
     }
+  } else if (LAYOUT == HEL_F32_PAIR) {
+    float2* p = static_cast<float2*>(f) + (long long)c * g.fs;   // pair (u_c, A_c)
+    float2 e = p[cell];
+    if (target) e.y = radd(e.y, (float)v);
+    else e.x = radd(e.x, (float)v);
+    ci.store(p, e);
   } else {
-    const long long e = (long long)c * g.fs + cell;   // pair (u_c, A_c), lane = target
-    if (LAYOUT == HEL_F32_PAIR) {
-      float* p = static_cast<float*>(f) + 2 * e + target;
-      *p = radd(*p, (float)v);
+    float4* p = static_cast<float4*>(f) + (long long)c * g.fs;   // dd2: (hi.x, hi.y, lo.x, lo.y)
+    float4 e = p[cell];
+    if (target) {
+      const dd w(__dadd_rn((double)e.y + (double)e.w, (double)v));
+      e.y = w.hi; e.w = w.lo;
     } else {
-      float* p = static_cast<float*>(f) + 4 * e + target;   // dd2: hi lanes at 0, 1; lo lanes at 2, 3
-      const dd w(__dadd_rn((double)p[0] + (double)p[2], (double)v));
-      p[0] = w.hi;
-      p[2] = w.lo;
+      const dd w(__dadd_rn((double)e.x + (double)e.z, (double)v));
+      e.x = w.hi; e.z = w.lo;
     }
+    ci.store(p, e);
   }
 }
 
@@ -144,52 +176,38 @@ __device__ __forceinline__ void add_field(void* f, const HelGeom& g, int target,
 // force goes into aa; uu receives forcing_rhs2 = Re[i coef3 fxyz] with coef3 =
 // crosshel k (k x (k x e)) (:1968, :2276-2281), zero for the default crosshel = 0,
 // so it is not applied.
+// One thread per interior cell: x from blockIdx.x/threadIdx.x, y = blockIdx.y, z = blockIdx.z.
 template <int LAYOUT, typename R>
 __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
-  const long long total = (long long)g.nx * g.ny * g.nz;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.nx) return;
   const int target = g.magnetic ? 1 : 0;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
-       q += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(q % g.nx);
-    const long long rr = q / g.nx;
-    const int j = (int)(rr % g.ny);
-    const int k = (int)(rr / g.ny);
-    const Images ix(i, g.nx), iy(j, g.ny), iz(k, g.nz);
-    const double* fx = tab + 8;
-    const double* fy = fx + 2 * g.nx;
-    const double* fz = fy + 2 * g.ny;
-    const R xr = (R)fx[2 * i], xi = (R)fx[2 * i + 1];
-    const R yr = (R)fy[2 * j], yi = (R)fy[2 * j + 1];
-    const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
-    const R pr = rsub(rmul(xr, yr), rmul(xi, yi)), pi = radd(rmul(xr, yi), rmul(xi, yr));   // fx fy
-    const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
-    R fc[3];
+  const double* fx = tab + 8;
+  const double* fy = fx + 2 * g.nx;
+  const double* fz = fy + 2 * g.ny;
+  const R xr = (R)fx[2 * i], xi = (R)fx[2 * i + 1];
+  const R yr = (R)fy[2 * j], yi = (R)fy[2 * j + 1];
+  const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
+  const R pr = rsub(rmul(xr, yr), rmul(xi, yi)), pi = radd(rmul(xr, yi), rmul(xi, yr));   // fx fy
+  const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
+  const CellImages ci(i, j, k, g);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) fc[c] = rsub(rmul((R)tab[c], qr), rmul((R)tab[3 + c], qi));
-    for (int a = 0; a < iz.n; ++a)
-      for (int b = 0; b < iy.n; ++b)
-        for (int e = 0; e < ix.n; ++e) {
-          const long long cell =
-              (long long)(iz.v[a] + 3) * g.ps + (long long)(iy.v[b] + 3) * g.px + g.xoff + ix.v[e];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) add_field<LAYOUT, R>(f, g, target, c, cell, fc[c]);
-        }
-  }
+  for (int c = 0; c < 3; ++c)
+    add_force<LAYOUT, R>(f, g, target, c, ci, rsub(rmul((R)tab[c], qr), rmul((R)tab[3 + c], qi)));
 }
 
 cudaError_t launch_helical(int layout, void* f, const HelRec* ring, const PcgbBoxState* state, double* tab,
                            const HelGeom& g, cudaStream_t s) {
+  if (g.ny > 65535 || g.nz > 65535) return cudaErrorInvalidValue;   // grid y/z limits
   helical_tables_kernel<<<1, 256, 0, s>>>(ring, state, tab, g);
-  const long long n = (long long)g.nx * g.ny * g.nz;
-  long long blocks = (n + 255) / 256;
-  if (blocks > 65535LL * 16) blocks = 65535LL * 16;
-  const int gb = (int)(blocks < 1 ? 1 : blocks);
+  const dim3 grid((unsigned)((g.nx + 127) / 128), (unsigned)g.ny, (unsigned)g.nz);
   switch (layout) {
-    case HEL_F32: helical_apply_kernel<HEL_F32, float><<<gb, 256, 0, s>>>(f, tab, g); break;
-    case HEL_F64: helical_apply_kernel<HEL_F64, double><<<gb, 256, 0, s>>>(f, tab, g); break;
-    case HEL_DD: helical_apply_kernel<HEL_DD, double><<<gb, 256, 0, s>>>(f, tab, g); break;
-    case HEL_F32_PAIR: helical_apply_kernel<HEL_F32_PAIR, float><<<gb, 256, 0, s>>>(f, tab, g); break;
-    default: helical_apply_kernel<HEL_DD_PAIR, double><<<gb, 256, 0, s>>>(f, tab, g); break;
+    case HEL_F32: helical_apply_kernel<HEL_F32, float><<<grid, 128, 0, s>>>(f, tab, g); break;
+    case HEL_F64: helical_apply_kernel<HEL_F64, double><<<grid, 128, 0, s>>>(f, tab, g); break;
+    case HEL_DD: helical_apply_kernel<HEL_DD, double><<<grid, 128, 0, s>>>(f, tab, g); break;
+    case HEL_F32_PAIR: helical_apply_kernel<HEL_F32_PAIR, float><<<grid, 128, 0, s>>>(f, tab, g); break;
+    default: helical_apply_kernel<HEL_DD_PAIR, double><<<grid, 128, 0, s>>>(f, tab, g); break;
   }
   return cudaGetLastError();
 }
