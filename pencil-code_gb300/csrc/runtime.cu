@@ -26,6 +26,7 @@
 
 #include "../../include/pcgb300.h"
 #include "aux_kernels.h"
+#include "cfl_pair.h"
 #include "helical.h"
 #include "kernels.cuh"
 #include "pcgb_box.h"
@@ -158,6 +159,9 @@ struct pcgb_box {
   int rng = 0;
   HelRec* dring = nullptr;
   double* dtab = nullptr;
+  // the CFL pass of the FP32 pair layout (cfl_pair.cu): per-block maxima and its counter
+  double* cfl_partial = nullptr;
+  unsigned int* cfl_done = nullptr;
 };
 
 // Element code of the layout kernels: float, double or double-float.
@@ -295,6 +299,7 @@ static void box_free(pcgb_box* b) {
   if (!b) return;
   cudaFree(b->f[0]); cudaFree(b->f[1]); cudaFree(b->df); cudaFree(b->forc); cudaFree(b->partial);
   cudaFree(b->dstate); cudaFree(b->ddev); cudaFree(b->dring); cudaFree(b->dtab);
+  cudaFree(b->cfl_partial); cudaFree(b->cfl_done);
   delete b;
 }
 
@@ -359,6 +364,12 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   if (cudaMalloc(&b->dring, sizeof(HelRec) * kHelRing) != cudaSuccess ||
       cudaMalloc(&b->dtab, sizeof(double) * (8 + 2 * ((size_t)b->nx + b->ny + b->nz))) != cudaSuccess)
     return fail("helical forcing tables");
+  if (b->tb == 4 && b->pairs) {
+    if (cudaMalloc(&b->cfl_partial, sizeof(double) * cfl_pair_blocks(b->nx, b->ny, b->nz)) != cudaSuccess ||
+        cudaMalloc(&b->cfl_done, sizeof(unsigned int)) != cudaSuccess)
+      return fail("CFL pass");
+    cudaMemsetAsync(b->cfl_done, 0, sizeof(unsigned int), g.stream);
+  }
   b->rng = p->seed_ff;
   cudaMemsetAsync(b->f[0], 0, b->fbytes, g.stream);
   cudaMemsetAsync(b->f[1], 0, b->fbytes, g.stream);
@@ -444,6 +455,11 @@ static bool box_needs_red(const pcgb_box* b, int mode) {
 }
 
 static int box_launch(pcgb_box* b, int mode) {
+  if (mode == MODE_CFL && b->cfl_partial) {   // FP32 pairs: the light CFL pass
+    CK(launch_cfl_pair(b->ddev, b->nf, b->nx, b->ny, b->nz, b->cfl_partial, b->cfl_done, g.stream));
+    ++g.launches;
+    return 0;
+  }
   const int rc = launch(b->ddev, 1, b->tiles, nullptr, mode, b->kh, b->tiles, box_needs_red(b, mode));
   if (mode == MODE_SUBSTEP && b->nsub % 3 == 0) b->diag_pending = false;
   return rc;

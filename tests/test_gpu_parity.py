@@ -255,3 +255,39 @@ def test_ragged_and_minimal_grids(pc, ic, orc, n, mode):
     err = rel_err(g, ref, LOG7 if mode.startswith("f32") else ())
     assert np.all(err <= tol), err
     assert np.array_equal(ic.fill_ghosts(g.copy()), g)
+
+
+@pytest.mark.parametrize("n,lentropy,tile", [((37, 19, 11), 0, 6), ((64, 40, 70), 0, 5), ((24, 16, 40), 1, 4)])
+def test_fp32_pair_cfl_pass(pc, ic, orc, n, lentropy, tile):
+    """The FP32 pair layout's own CFL pass (dt from the current f) against the
+    oracle's set_dt1_max on the same state, on ragged grids and with entropy."""
+    kw = dict(lentropy=1, gamma=5.0 / 3.0, chi=0.02) if lentropy else {}
+    p = iso_params(pc, precision=4, comp=1, tile=tile, dt=0.0, dt_mode=2, cdt=0.4, b_ext=(0.05, 0.0, 0.1),
+                   nu=0.02, eta=0.03, **kw).update(nx=n[0], ny=n[1], nz=n[2])
+    f0 = ic.zeros(p)
+    ic.gaussian_noise(f0, p, ["ux", "uy", "uz", "ax", "ay", "az", "lnrho"] + (["ss"] if lentropy else []), 5e-2, 43)
+    ic.fill_ghosts(f0)
+    box = pc.Box(p)
+    box.load(f0)
+    box.steps(1)
+    t, dt, _ = box.time()
+    op = oracle_params(orc, p)
+    f = np.array(f0, order="F", copy=True)
+    orc.ghosts(op, f)
+    dt1, _ = orc.pde(op, f, np.zeros_like(f), 0.0, want_dt=True)
+    assert abs(dt * dt1 - 1.0) <= 2e-6
+    assert abs(t - dt) <= 1e-15 * dt
+
+
+def test_fp32_pair_cfl_pass_flags_nan(pc, ic):
+    L = pc.load()
+    p = iso_params(pc, precision=4, comp=1, tile=5, dt=0.0, dt_mode=2)
+    f = ic.zeros(p)
+    ic.gaussian_noise(f, p, ["ux", "uy", "uz"], 1e-2, 3)
+    f[7, 9, 11, 5] = np.nan   # A_y: reaches dt only through B
+    box = pc.Box(p)
+    box.load(f)
+    box.steps(1)
+    with pytest.raises(pc.PcgbError, match="non-finite"):
+        box.sync()
+    L.pcgb_clear_error()
