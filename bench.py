@@ -342,9 +342,7 @@ def run_ours(args):
     # ---- e2e through the plug-in C ABI with pinned host buffers ----
     e2e = None
     if not args.no_e2e:
-        if timings:
-            L.pcgb_set_kvectors(kvec.ctypes.data_as(C.POINTER(C.c_double)), kvec.shape[1], kav)
-        e2e = run_e2e(args, pc, gpu, torch, stream, p, nf, ws)
+        e2e = run_e2e(args, pc, gpu, torch, stream, p, nf, ws, kvec=(kvec, kav) if timings else None)
 
     # ---- CPU baseline (rank 0, N=1 only) ----
     cpu = None
@@ -389,10 +387,26 @@ def run_ours(args):
     return 0
 
 
-def run_e2e(args, pc, gpu, torch, stream, p, nf, ws: int = 1):
+def _ck(L, rc: int) -> None:
+    """Raise for a non-zero status of library L (the double or the single-precision build)."""
+    if rc:
+        msg = L.pcgb_error_string(rc).decode()
+        L.pcgb_clear_error()
+        raise RuntimeError(f"pcgb error {rc}: {msg}")
+
+
+def run_e2e(args, pc, gpu, torch, stream, p, nf, ws: int = 1, kvec=None):
+    """The metric through the reference plug-in ABI with a page-locked host f-array of the
+    Fortran build's REAL: float for an FP32 device state (libpcgb300_sgl.so, the
+    single-precision build), double otherwise (libpcgb300.so)."""
+    lib = importlib.import_module("pencil-code_gb300.lib")
+    single = p.precision == 4
+    L = lib.load_sgl() if single else pc.load()
+    real, hbytes = (C.c_float, 4) if single else (C.c_double, 8)
+    rptr = C.POINTER(real)
     n = p.nx
     shape = (n + 6, n + 6, n + 6, nf)
-    nbytes = int(np.prod(shape)) * 8
+    nbytes = int(np.prod(shape)) * hbytes
     try:
         avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
     except Exception:
@@ -407,18 +421,24 @@ def run_e2e(args, pc, gpu, torch, stream, p, nf, ws: int = 1):
     if not fits:
         return {"value": None, "unit": "Gcell-updates/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                 "note": f"host f-array of {nbytes / 1e9:.1f} GB x {ws} ranks exceeds the host memory budget"}
-    ht = torch.zeros(int(np.prod(shape)), dtype=torch.float64, pin_memory=True)
+    ht = torch.zeros(int(np.prod(shape)), dtype=torch.float32 if single else torch.float64, pin_memory=True)
     fh = ht.numpy().reshape(shape, order="F")
     iax = 5 if p.lentropy else 4
     rng = np.random.Generator(np.random.PCG64(7))
     for k in range(3):
         fh[3:-3, 3:-3, 3:-3, iax + k] = 1e-5 * rng.standard_normal((n, n, n))
-    L = pc.load()
-    gpu.initialize_gpu(fh, p, t=0.0, nt=0)
-    red = np.zeros(gpu.n_gpu_reduced_vars)
-    rp = red.ctypes.data_as(C.POINTER(C.c_double))
+    L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
+    if kvec is not None:
+        kv = np.ascontiguousarray(kvec[0])
+        _ck(L, L.pcgb_set_kvectors(kv.ctypes.data_as(C.POINTER(C.c_double)), kv.shape[1], kvec[1]))
+    _ck(L, L.pcgb_set_params(C.byref(p)))
+    fptr = fh.ctypes.data_as(rptr)
+    L.initializeGPU(fptr, 0, 0.0, 0, 0, 0, 0)
+    _ck(L, L.pcgb_last_error())
+    red = np.zeros(gpu.n_gpu_reduced_vars, dtype=np.float32 if single else np.float64)
+    rp = red.ctypes.data_as(rptr)
     # warm-up through the same calls
-    gpu.load_farray_to_gpu()
+    L.loadFarray()
     for _ in range(args.warmup):
         for s in (1, 2, 3):
             L.substepGPU(s, 0.0)
@@ -426,22 +446,23 @@ def run_e2e(args, pc, gpu, torch, stream, p, nf, ws: int = 1):
     if ws > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
-    gpu.load_farray_to_gpu()
+    L.loadFarray()
     for _ in range(args.steps):
         for s in (1, 2, 3):
             L.substepGPU(s, 0.0)
         L.getGPUReducedVars(rp)
-    gpu.copy_farray_from_gpu(fh)
+    L.copyFarray(fptr)
     torch.cuda.synchronize()
     el = max_over_ranks(time.perf_counter() - t0, device="cuda")
-    gpu.finalize_gpu()
+    _ck(L, L.pcgb_last_error())
+    L.finalizeGPU()
     cells = float(n) ** 3
     # whole job: every rank advances its own replica through its own host array
     return {"value": ws * cells * 3 * args.steps / el / 1e9, "unit": "Gcell-updates/s",
             "h2d_bytes_per_step": ws * nbytes / args.steps,
             "d2h_bytes_per_step": ws * (nbytes / args.steps + red.nbytes),
             "what": "loadFarray + K x (substepGPU x3 + getGPUReducedVars) + copyFarray, pinned host f-array "
-                    "(REAL=double), wall clock"}
+                    f"(REAL={'float, libpcgb300_sgl.so' if single else 'double, libpcgb300.so'}), wall clock"}
 
 
 def run_ensemble(args):

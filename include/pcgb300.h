@@ -32,7 +32,15 @@
 extern "C" {
 #endif
 
-typedef double REAL_PCGB; /* REAL of the double build */
+/* REAL of the Fortran build the plug-in entry points serve (headers_c.h:11-25):
+   double in libpcgb300.so (REAL_PRECISION=double), float in libpcgb300_sgl.so,
+   the same library compiled with PCGB_REAL_SINGLE for the single-precision
+   build.  The device state's precision is pcgb_params.precision in both. */
+#ifdef PCGB_REAL_SINGLE
+typedef float REAL_PCGB;
+#else
+typedef double REAL_PCGB;
+#endif
 
 /* ---------------------------------------------------------------------------
  * Parameter block.  Field meanings follow the reference namelists:
@@ -223,9 +231,14 @@ typedef struct pcgb_batch pcgb_batch;
 
 pcgb_box* pcgb_box_create(const pcgb_params* p);
 void pcgb_box_destroy(pcgb_box* b);
-/* f(mx,my,mz,nf) double, Fortran order, ghosts included (ghosts are refreshed on device). */
+/* f(mx,my,mz,nf) double, Fortran order, ghosts included (ghosts are refreshed on device).
+   Page-locked host arrays are read or written in place by the layout kernels. */
 int pcgb_box_load(pcgb_box* b, const double* f_host, double t);
 int pcgb_box_store(pcgb_box* b, double* f_host);
+/* The same with a float host f-array (the single-precision Fortran build).  The
+   store rounds f (+ the FP32 compensation carry, summed in double) once to float. */
+int pcgb_box_load_f32(pcgb_box* b, const float* f_host, double t);
+int pcgb_box_store_f32(pcgb_box* b, float* f_host);
 /* Seeded initial condition written on the device (for boxes too large to
    stage through host memory): kind 0 sets field to zero, 1 adds ampl*N(0,1)
    from a counter-based generator seeded by seed, 2 adds component `field`

@@ -1,8 +1,10 @@
 """Build recipe for libpcgb300.so (sm_103a) -- nvcc only, no cmake.
 
 Compiles the kernel translation units in parallel into ``_build/`` next to
-this file and links them into ``_build/libpcgb300.so``.  Re-running only
-recompiles sources newer than their objects.
+this file and links them into ``_build/libpcgb300.so`` (plug-in entry points
+with REAL = double) and ``_build/libpcgb300_sgl.so`` (the same library with
+the runtime compiled for REAL = float, the single-precision Fortran build).
+Re-running only recompiles sources newer than their objects.
 """
 from __future__ import annotations
 
@@ -15,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpcgb300.so")
+LIB_SGL = os.path.join(OUT, "libpcgb300_sgl.so")
+# translation units compiled a second time for the single-precision plug-in
+SGL_SOURCES = {"runtime.cu": "runtime_sgl.o"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["kernels_f32_7.cu", "kernels_f32_8.cu", "kernels_f64_7.cu", "kernels_f64_8.cu", "kernels_dd_7.cu",
            "kernels_dd_8.cu", "kernels_upw_f32.cu", "kernels_upw_f64.cu", "kernels_upw_dd.cu", "helical.cu", "cfl_pair.cu",
@@ -52,13 +57,13 @@ def _newest_dep() -> float:
     return max(os.path.getmtime(d) for d in deps if os.path.exists(d))
 
 
-def _compile(src: str, verbose: bool) -> str:
-    obj = os.path.join(OUT, src.replace(".cu", ".o"))
+def _compile(src: str, verbose: bool, obj_name: str | None = None, defines: tuple[str, ...] = ()) -> str:
+    obj = os.path.join(OUT, obj_name or src.replace(".cu", ".o"))
     path = os.path.join(CSRC, src)
     if (os.path.exists(obj) and _elf_machine_ok(obj)
             and os.path.getmtime(obj) >= max(os.path.getmtime(path), _newest_dep())):
         return obj
-    cmd = [nvcc(), *_flags(), "-c", path, "-o", obj]
+    cmd = [nvcc(), *_flags(), *[f"-D{d}" for d in defines], "-c", path, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -67,19 +72,29 @@ def _compile(src: str, verbose: bool) -> str:
     return obj
 
 
+def _link(lib: str, objs: list[str], verbose: bool) -> None:
+    if (os.path.exists(lib) and _elf_machine_ok(lib)
+            and os.path.getmtime(lib) >= max(os.path.getmtime(o) for o in objs)):
+        return
+    cmd = [nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-lcudart"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
-    with cf.ThreadPoolExecutor(max_workers=max(1, min(os.cpu_count() or 4, len(srcs)))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
-    if (not os.path.exists(LIB) or not _elf_machine_ok(LIB)
-            or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs)):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    jobs = [(s, None, ()) for s in srcs] + [(s, o, ("PCGB_REAL_SINGLE",)) for s, o in SGL_SOURCES.items()]
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(os.cpu_count() or 4, len(jobs)))) as ex:
+        objs = list(ex.map(lambda j: _compile(j[0], verbose, j[1], j[2]), jobs))
+    common = objs[:len(srcs)]
+    sgl = objs[len(srcs):]
+    _link(LIB, common, verbose)
+    swap = {os.path.join(OUT, s.replace(".cu", ".o")): o for s, o in zip(SGL_SOURCES, sgl)}
+    _link(LIB_SGL, [swap.get(o, o) for o in common], verbose)
     return LIB
 
 

@@ -59,23 +59,25 @@ __device__ __forceinline__ long long dev_index(long long row, int i, int my, int
   return 2 * (((long long)pair * my * mz + jk) * px + xoff - 3 + i) + lane;
 }
 
-// Rows [r0, r0+nr) of the host layout (double) -> device layout (T).
-template <typename T>
-__global__ void load_rows_kernel(T* __restrict__ f, const double* __restrict__ stage, long long r0, long long nr, int mx,
+// Rows [r0, r0+nr) of the host layout (REAL H: double, or float for the
+// single-precision build) -> device layout (T).
+template <typename T, typename H>
+__global__ void load_rows_kernel(T* __restrict__ f, const H* __restrict__ stage, long long r0, long long nr, int mx,
                                  int my, int mz, int px, int xoff, int nf, int pairs) {
   const long long total = nr * mx;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
     const long long r = q / mx;
     const int i = (int)(q - r * mx);
-    f[dev_index(r0 + r, i, my, mz, px, xoff, nf, pairs)] = (T)stage[q];
+    f[dev_index(r0 + r, i, my, mz, px, xoff, nf, pairs)] = T((double)stage[q]);
   }
 }
 
-// Device layout (T) -> host-layout rows (double).  With a carry array (FP32
-// compensated mode), the value returned is f + carry of the interior image.
-template <typename T>
-__global__ void store_rows_kernel(double* __restrict__ stage, const T* __restrict__ f, const T* __restrict__ carry,
+// Device layout (T) -> host-layout rows (REAL H).  With a carry array (FP32
+// compensated mode), the value returned is f + carry of the interior image,
+// summed in double and rounded once to H.
+template <typename T, typename H>
+__global__ void store_rows_kernel(H* __restrict__ stage, const T* __restrict__ f, const T* __restrict__ carry,
                                   long long r0, long long nr, int nx, int ny, int nz, int px, int my, int mz,
                                   int xoff, int nf, int pairs) {
   const int mx = nx + 6;
@@ -94,13 +96,14 @@ __global__ void store_rows_kernel(double* __restrict__ stage, const T* __restric
       const long long crow = (long long)(wrap(j, ny) + 3) + (long long)my * ((wrap(k, nz) + 3) + (long long)mz * fld);
       v += (double)carry[dev_index(crow, wrap(i, nx) + 3, my, mz, px, xoff, nf, pairs)];
     }
-    stage[q] = v;
+    stage[q] = (H)v;
   }
 }
 
 // Double-float pair layout: device element e of 16 bytes holds (hi_a, hi_b,
 // lo_a, lo_b); dev_index's pair index 2e + lane selects the field.
-__global__ void load_rows_ddpair_kernel(float* __restrict__ f, const double* __restrict__ stage, long long r0,
+template <typename H>
+__global__ void load_rows_ddpair_kernel(float* __restrict__ f, const H* __restrict__ stage, long long r0,
                                         long long nr, int mx, int my, int mz, int px, int xoff, int nf) {
   const long long total = nr * mx;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
@@ -109,13 +112,14 @@ __global__ void load_rows_ddpair_kernel(float* __restrict__ f, const double* __r
     const int i = (int)(q - r * mx);
     const long long pi = dev_index(r0 + r, i, my, mz, px, xoff, nf, 1);
     const long long e = pi >> 1, lane = pi & 1;
-    const dd v(stage[q]);
+    const dd v((double)stage[q]);
     f[4 * e + lane] = v.hi;
     f[4 * e + 2 + lane] = v.lo;
   }
 }
 
-__global__ void store_rows_ddpair_kernel(double* __restrict__ stage, const float* __restrict__ f, long long r0,
+template <typename H>
+__global__ void store_rows_ddpair_kernel(H* __restrict__ stage, const float* __restrict__ f, long long r0,
                                          long long nr, int nx, int my, int mz, int px, int xoff, int nf) {
   const int mx = nx + 6;
   const long long total = nr * mx;
@@ -125,7 +129,7 @@ __global__ void store_rows_ddpair_kernel(double* __restrict__ stage, const float
     const int i = (int)(q - r * mx);
     const long long pi = dev_index(r0 + r, i, my, mz, px, xoff, nf, 1);
     const long long e = pi >> 1, lane = pi & 1;
-    stage[q] = (double)f[4 * e + lane] + (double)f[4 * e + 2 + lane];
+    stage[q] = (H)((double)f[4 * e + lane] + (double)f[4 * e + 2 + lane]);
   }
 }
 
@@ -149,35 +153,51 @@ cudaError_t launch_ghost_fill(int tbytes, void* f, int nx, int ny, int nz, int p
   return cudaGetLastError();
 }
 
-cudaError_t launch_load_rows(int tbytes, void* f, const double* stage, long long r0, long long nr, int mx, int my,
-                             int mz, int px, int xoff, int nf, int pairs, cudaStream_t s) {
+template <typename H>
+static void load_rows(int tbytes, void* f, const H* stage, long long r0, long long nr, int mx, int my, int mz, int px,
+                      int xoff, int nf, int pairs, cudaStream_t s) {
   const int th = 256, g = grid_for(nr * mx, th);
   if (tbytes == 4)
-    load_rows_kernel<float><<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
+    load_rows_kernel<float, H><<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
   else if (tbytes == kElemDD)
-    load_rows_kernel<dd><<<g, th, 0, s>>>((dd*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
+    load_rows_kernel<dd, H><<<g, th, 0, s>>>((dd*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
   else if (tbytes == kElemDDPair)
-    load_rows_ddpair_kernel<<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, my, mz, px, xoff, nf);
+    load_rows_ddpair_kernel<H><<<g, th, 0, s>>>((float*)f, stage, r0, nr, mx, my, mz, px, xoff, nf);
   else
-    load_rows_kernel<double><<<g, th, 0, s>>>((double*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
+    load_rows_kernel<double, H><<<g, th, 0, s>>>((double*)f, stage, r0, nr, mx, my, mz, px, xoff, nf, pairs);
+}
+
+cudaError_t launch_load_rows(int tbytes, int hbytes, void* f, const void* stage, long long r0, long long nr, int mx,
+                             int my, int mz, int px, int xoff, int nf, int pairs, cudaStream_t s) {
+  if (hbytes == 4) load_rows(tbytes, f, (const float*)stage, r0, nr, mx, my, mz, px, xoff, nf, pairs, s);
+  else load_rows(tbytes, f, (const double*)stage, r0, nr, mx, my, mz, px, xoff, nf, pairs, s);
   return cudaGetLastError();
 }
 
-cudaError_t launch_store_rows(int tbytes, double* stage, const void* f, const void* carry, long long r0, long long nr,
-                              int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs,
-                              cudaStream_t s) {
+template <typename H>
+static void store_rows(int tbytes, H* stage, const void* f, const void* carry, long long r0, long long nr, int nx,
+                       int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs, cudaStream_t s) {
   const int th = 256, g = grid_for(nr * (nx + 6), th);
   if (tbytes == 4)
-    store_rows_kernel<float><<<g, th, 0, s>>>(stage, (const float*)f, (const float*)carry, r0, nr, nx, ny, nz, px, my,
-                                              mz, xoff, nf, pairs);
+    store_rows_kernel<float, H><<<g, th, 0, s>>>(stage, (const float*)f, (const float*)carry, r0, nr, nx, ny, nz, px,
+                                                 my, mz, xoff, nf, pairs);
   else if (tbytes == kElemDD)
-    store_rows_kernel<dd><<<g, th, 0, s>>>(stage, (const dd*)f, nullptr, r0, nr, nx, ny, nz, px, my, mz, xoff, nf,
-                                           pairs);
+    store_rows_kernel<dd, H><<<g, th, 0, s>>>(stage, (const dd*)f, nullptr, r0, nr, nx, ny, nz, px, my, mz, xoff, nf,
+                                              pairs);
   else if (tbytes == kElemDDPair)
-    store_rows_ddpair_kernel<<<g, th, 0, s>>>(stage, (const float*)f, r0, nr, nx, my, mz, px, xoff, nf);
+    store_rows_ddpair_kernel<H><<<g, th, 0, s>>>(stage, (const float*)f, r0, nr, nx, my, mz, px, xoff, nf);
   else
-    store_rows_kernel<double><<<g, th, 0, s>>>(stage, (const double*)f, (const double*)carry, r0, nr, nx, ny, nz, px,
-                                               my, mz, xoff, nf, pairs);
+    store_rows_kernel<double, H><<<g, th, 0, s>>>(stage, (const double*)f, (const double*)carry, r0, nr, nx, ny, nz,
+                                                  px, my, mz, xoff, nf, pairs);
+}
+
+cudaError_t launch_store_rows(int tbytes, int hbytes, void* stage, const void* f, const void* carry, long long r0,
+                              long long nr, int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs,
+                              cudaStream_t s) {
+  if (hbytes == 4)
+    store_rows(tbytes, (float*)stage, f, carry, r0, nr, nx, ny, nz, px, my, mz, xoff, nf, pairs, s);
+  else
+    store_rows(tbytes, (double*)stage, f, carry, r0, nr, nx, ny, nz, px, my, mz, xoff, nf, pairs, s);
   return cudaGetLastError();
 }
 

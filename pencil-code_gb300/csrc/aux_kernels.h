@@ -12,10 +12,11 @@ constexpr int kElemDDPair = 32;
 cudaError_t launch_ghost_fill(int tbytes, void* f, int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf,
                               cudaStream_t s);
 // pairs = 1: packed field-pair layout (P0=(ux,ax) P1=(uy,ay) P2=(uz,az) P3=(lnrho,ss)), px/xoff in pair units
-cudaError_t launch_load_rows(int tbytes, void* f, const double* stage, long long r0, long long nr, int mx, int my,
-                             int mz, int px, int xoff, int nf, int pairs, cudaStream_t s);
-cudaError_t launch_store_rows(int tbytes, double* stage, const void* f, const void* carry, long long r0, long long nr,
-                              int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs,
+// Host rows of REAL type (hbytes 8: double, 4: float) <-> the device layout.
+cudaError_t launch_load_rows(int tbytes, int hbytes, void* f, const void* stage, long long r0, long long nr, int mx,
+                             int my, int mz, int px, int xoff, int nf, int pairs, cudaStream_t s);
+cudaError_t launch_store_rows(int tbytes, int hbytes, void* stage, const void* f, const void* carry, long long r0,
+                              long long nr, int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs,
                               cudaStream_t s);
 }  // namespace pcgb
 namespace pcgb {

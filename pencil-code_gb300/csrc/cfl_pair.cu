@@ -9,8 +9,10 @@
 // (x, y) column of a z-chunk: the z-derivatives of A_x and A_y come from
 // 7-plane register windows, the x- and y-derivatives of A from neighbouring
 // elements read through L1 (ghost zones are the periodic images kept by the
-// substep kernel).  The derivative arithmetic is PairCell::St::der's on the
-// A lanes, so the per-cell values, and the maximum, are the fused pass's.
+// substep kernel); each thread requests its column kPF planes ahead into L2,
+// so the loads of a plane meet L2 rather than HBM latency.  The derivative
+// arithmetic is PairCell::St::der's on the A lanes, so the per-cell values,
+// and the maximum, are the fused pass's.
 #include "cell_pair.cuh"
 #include "cfl_pair.h"
 
@@ -20,6 +22,7 @@ namespace {
 
 constexpr int kTX = 32, kTY = 8, kZC = 32;   // block (x, y) and z-chunk
 constexpr int kThreads = kTX * kTY;
+constexpr int kPF = 4;   // the column's lines are requested into L2 this many planes ahead
 
 // der_main (deriv.f90:127-129) on single values, in PairCell::St::der's order
 __device__ __forceinline__ float der1(float m3, float m2, float m1, float p1, float p2, float p3, float fac) {
@@ -31,7 +34,7 @@ __device__ __forceinline__ float der1(float m3, float m2, float m1, float p1, fl
 __device__ __forceinline__ float nanmax(float a, float b) { return (b > a || b != b) ? b : a; }
 
 template <int NF>
-__global__ void __launch_bounds__(kThreads) cfl_pair_kernel(const PcgbBoxDev* __restrict__ Bp, double* partial,
+__global__ void __launch_bounds__(kThreads, 3) cfl_pair_kernel(const PcgbBoxDev* __restrict__ Bp, double* partial,
                                                              unsigned int* done) {
   const PcgbBoxDev& B = *Bp;
   PcgbBoxState* const S = B.state;
@@ -60,6 +63,10 @@ __global__ void __launch_bounds__(kThreads) cfl_pair_kernel(const PcgbBoxDev* __
       ay[k] = __ldg(&col1[(long long)(z0 + k) * ps].y);
     }
     for (int z = z0; z < z1; ++z) {
+      if (z + 3 + kPF < B.mz) {   // every pair of this column, kPF planes ahead
+#pragma unroll
+        for (int p = 0; p < 4; ++p) prefetch_l2(col + p * fs + (long long)(z + 3 + kPF) * ps);
+      }
       ax[6] = __ldg(&col[(long long)(z + 6) * ps].y);
       ay[6] = __ldg(&col1[(long long)(z + 6) * ps].y);
       const float2* const q = col + (long long)(z + 3) * ps;   // this cell, pair 0

@@ -522,14 +522,15 @@ static const void* host_alias(const void* h) {
   return nullptr;
 }
 
-extern "C" int pcgb_box_load(pcgb_box* b, const double* fh, double t) {
+// Host f-array of REAL type (hb = 8: double, 4: float) into the box.
+static int box_load_host(pcgb_box* b, const void* fh, int hb, double t) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!b || !fh) return set_err(PCGB_E_ARG, "null argument");
   const long long rows = (long long)b->my * b->mz * b->nf;
   const int in = cur_in(b);
   if (const void* dh = host_alias(fh)) {
-    CK(launch_load_rows(elem_code(b), b->f[in], static_cast<const double*>(dh), 0, rows, b->mx, b->my, b->mz, b->px,
-                        b->xoff, b->nf, b->pairs, g.stream));
+    CK(launch_load_rows(elem_code(b), hb, b->f[in], dh, 0, rows, b->mx, b->my, b->mz, b->px, b->xoff, b->nf, b->pairs,
+                        g.stream));
     ++g.launches;
     return box_reset(b, t);
   }
@@ -543,17 +544,20 @@ extern "C" int pcgb_box_load(pcgb_box* b, const double* fh, double t) {
     const int k = c & 1;
     const long long nr = std::min(chunk, rows - r0);
     CK(cudaStreamWaitEvent(g.xfer, g.ev_free[k], 0));
-    CK(cudaMemcpyAsync(g.stage[k], fh + r0 * b->mx, (size_t)(nr * b->mx) * sizeof(double), cudaMemcpyHostToDevice,
-                       g.xfer));
+    CK(cudaMemcpyAsync(g.stage[k], static_cast<const char*>(fh) + (size_t)(r0 * b->mx) * hb, (size_t)(nr * b->mx) * hb,
+                       cudaMemcpyHostToDevice, g.xfer));
     CK(cudaEventRecord(g.ev_copied[k], g.xfer));
     CK(cudaStreamWaitEvent(g.stream, g.ev_copied[k], 0));
-    CK(launch_load_rows(elem_code(b), b->f[in], g.stage[k], r0, nr, b->mx, b->my, b->mz, b->px, b->xoff, b->nf, b->pairs,
-                        g.stream));
+    CK(launch_load_rows(elem_code(b), hb, b->f[in], g.stage[k], r0, nr, b->mx, b->my, b->mz, b->px, b->xoff, b->nf,
+                        b->pairs, g.stream));
     CK(cudaEventRecord(g.ev_free[k], g.stream));
     ++g.launches;
   }
   return box_reset(b, t);
 }
+
+extern "C" int pcgb_box_load(pcgb_box* b, const double* fh, double t) { return box_load_host(b, fh, 8, t); }
+extern "C" int pcgb_box_load_f32(pcgb_box* b, const float* fh, double t) { return box_load_host(b, fh, 4, t); }
 
 // Seeded initial condition on the device (kind 0 zero, 1 Gaussian noise of
 // amplitude ampl, 2 ABC flow component `field` 0..2 with a,b,c,k), then the
@@ -584,7 +588,8 @@ extern "C" int pcgb_box_init_field(pcgb_box* b, int field, int kind, double ampl
   return box_reset(b, 0.0);
 }
 
-extern "C" int pcgb_box_store(pcgb_box* b, double* fh) {
+// The box's f into a host f-array of REAL type (hb = 8: double, 4: float).
+static int box_store_host(pcgb_box* b, void* fh, int hb) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!b || !fh) return set_err(PCGB_E_ARG, "null argument");
   const long long rows = (long long)b->my * b->mz * b->nf;
@@ -592,7 +597,7 @@ extern "C" int pcgb_box_store(pcgb_box* b, double* fh) {
   // the FP32 carry lives in df between steps (substep counter at a step boundary)
   const void* carry = (b->hdev.comp && (b->nsub % 3) == 0) ? b->df : nullptr;
   if (void* dh = const_cast<void*>(host_alias(fh))) {
-    CK(launch_store_rows(elem_code(b), static_cast<double*>(dh), b->f[in], carry, 0, rows, b->nx, b->ny, b->nz, b->px,
+    CK(launch_store_rows(elem_code(b), hb, dh, b->f[in], carry, 0, rows, b->nx, b->ny, b->nz, b->px,
                          b->my, b->mz, b->xoff, b->nf, b->pairs, g.stream));
     ++g.launches;
     CK(cudaStreamSynchronize(g.stream));
@@ -607,19 +612,22 @@ extern "C" int pcgb_box_store(pcgb_box* b, double* fh) {
     const int k = c & 1;
     const long long nr = std::min(chunk, rows - r0);
     CK(cudaStreamWaitEvent(g.stream, g.ev_free[k], 0));
-    CK(launch_store_rows(elem_code(b), g.stage[k], b->f[in], carry, r0, nr, b->nx, b->ny, b->nz, b->px, b->my, b->mz,
+    CK(launch_store_rows(elem_code(b), hb, g.stage[k], b->f[in], carry, r0, nr, b->nx, b->ny, b->nz, b->px, b->my, b->mz,
                          b->xoff, b->nf, b->pairs, g.stream));
     ++g.launches;
     CK(cudaEventRecord(g.ev_copied[k], g.stream));
     CK(cudaStreamWaitEvent(g.xfer, g.ev_copied[k], 0));
-    CK(cudaMemcpyAsync(fh + r0 * b->mx, g.stage[k], (size_t)(nr * b->mx) * sizeof(double), cudaMemcpyDeviceToHost,
-                       g.xfer));
+    CK(cudaMemcpyAsync(static_cast<char*>(fh) + (size_t)(r0 * b->mx) * hb, g.stage[k], (size_t)(nr * b->mx) * hb,
+                       cudaMemcpyDeviceToHost, g.xfer));
     CK(cudaEventRecord(g.ev_free[k], g.xfer));
   }
   CK(cudaStreamSynchronize(g.xfer));
   CK(cudaStreamSynchronize(g.stream));
   return box_check_state(b);
 }
+
+extern "C" int pcgb_box_store(pcgb_box* b, double* fh) { return box_store_host(b, fh, 8); }
+extern "C" int pcgb_box_store_f32(pcgb_box* b, float* fh) { return box_store_host(b, fh, 4); }
 
 // Layout code of the helical forcing kernels.
 static int hel_layout(const pcgb_box* b) {
@@ -993,7 +1001,14 @@ static bool g_par_set = false;
 static pcgb_box* g_box = nullptr;
 static std::vector<double> g_kvec;   // k.dat of the plug-in's box
 static double g_kav = 0.0;
-static double* g_hostf = nullptr;
+static REAL_PCGB* g_hostf = nullptr;
+
+// The plug-in's host f-array is the Fortran build's REAL (double, or float in
+// the single-precision library).
+static int host_load(pcgb_box* b, const double* f, double t) { return pcgb_box_load(b, f, t); }
+static int host_load(pcgb_box* b, const float* f, double t) { return pcgb_box_load_f32(b, f, t); }
+static int host_store(pcgb_box* b, double* f) { return pcgb_box_store(b, f); }
+static int host_store(pcgb_box* b, float* f) { return pcgb_box_store_f32(b, f); }
 
 extern "C" int pcgb_set_params(const pcgb_params* p) {
   if (validate(p)) return g_err;
@@ -1018,7 +1033,7 @@ extern "C" void initializeGPU(REAL_PCGB* f, int comm, double t, int nt, int read
   if (!g_box) return;
   if (!g_kvec.empty()) pcgb_box_set_kvectors(g_box, g_kvec.data(), (int)(g_kvec.size() / 3), g_kav);
   g_hostf = f;
-  if (f && nt > 0) pcgb_box_load(g_box, f, t);   // gpu_astaroth.f90:236 load_farray_to_GPU
+  if (f && nt > 0) host_load(g_box, f, t);   // gpu_astaroth.f90:236 load_farray_to_GPU
   else if (g_box) {
     PcgbBoxState st;
     cudaMemcpy(&st, g_box->dstate, sizeof(st), cudaMemcpyDeviceToHost);
@@ -1059,14 +1074,14 @@ extern "C" void radTransfer(void) {}
 extern "C" void copyFarray(REAL_PCGB* f) {
   if (!g_box) { set_err(PCGB_E_STATE, "copyFarray before initializeGPU"); return; }
   if (!f) f = g_hostf;
-  if (f) pcgb_box_store(g_box, f);
+  if (f) host_store(g_box, f);
 }
 
 extern "C" void loadFarray(void) {
   if (!g_box || !g_hostf) { set_err(PCGB_E_STATE, "loadFarray without a bound host f-array"); return; }
   double t = 0;
   pcgb_box_time(g_box, &t, nullptr, nullptr);
-  pcgb_box_load(g_box, g_hostf, t);
+  host_load(g_box, g_hostf, t);
 }
 
 static int box_reload(pcgb_box* b, const pcgb_params& p) {
@@ -1114,9 +1129,10 @@ static int par_find(const char* name) {
     if (strcmp(kPar[i].name, name) == 0) return i;
   return -1;
 }
-static void par_set(int i, const double* v, int n) {
+// values of the Fortran REAL type (double or float) into the double parameters
+static void par_set(int i, const REAL_PCGB* v, int n) {
   double* dst = reinterpret_cast<double*>(reinterpret_cast<char*>(&g_par) + kPar[i].off);
-  for (int k = 0; k < kPar[i].n && k < n; ++k) dst[k] = v[k];
+  for (int k = 0; k < kPar[i].n && k < n; ++k) dst[k] = (double)v[k];
   if (g_box) box_reload(g_box, g_par);
 }
 

@@ -11,6 +11,7 @@ import os
 import numpy as np
 
 from .build import LIB as _LIB
+from .build import LIB_SGL as _LIB_SGL
 from .build import build as _do_build
 
 NSLOT = 10
@@ -80,7 +81,8 @@ EXPORTS = [
     "tf_load_model_checkpoint_c_", "tf_save_model_c_", "tf_save_checkpoint_c_",
     "pcgb_box_set_kvectors", "pcgb_set_kvectors",
     "pcgb_get_dt", "pcgb_get_time", "pcgb_request_diagnostics", "pcgb_time_step",
-    "pcgb_box_create", "pcgb_box_destroy", "pcgb_box_load", "pcgb_box_store", "pcgb_box_init_field", "pcgb_box_steps",
+    "pcgb_box_create", "pcgb_box_destroy", "pcgb_box_load", "pcgb_box_store", "pcgb_box_load_f32",
+    "pcgb_box_store_f32", "pcgb_box_init_field", "pcgb_box_steps",
     "pcgb_box_sync", "pcgb_box_diag", "pcgb_box_time", "pcgb_box_set_dt", "pcgb_box_bytes",
     "pcgb_box_info", "pcgb_batch_create", "pcgb_batch_destroy", "pcgb_batch_steps", "pcgb_autotune",
     "pcgb_launch_count", "pcgb_version", "pcgb_substep_noalloc", "pcgb_params_bytes", "pcgb_set_wait_limit", "pcgb_inject_wait_failure",
@@ -96,9 +98,25 @@ def lib_path() -> str:
 def load(build_if_missing: bool = True) -> C.CDLL:
     """Load libpcgb300.so (building it first if asked and absent)."""
     global _lib
-    if _lib is not None:
-        return _lib
-    path = lib_path()
+    if _lib is None:
+        _lib = _open(lib_path(), C.c_double, build_if_missing)
+    return _lib
+
+
+def load_sgl(build_if_missing: bool = True) -> C.CDLL:
+    """Load libpcgb300_sgl.so: the plug-in entry points with REAL = float, for
+    the reference's single-precision build (a library of its own, with its own
+    engine state, as the reference links libastaroth_sgl.so)."""
+    global _lib_sgl
+    if _lib_sgl is None:
+        _lib_sgl = _open(_LIB_SGL, C.c_float, build_if_missing)
+    return _lib_sgl
+
+
+_lib_sgl = None
+
+
+def _open(path: str, real, build_if_missing: bool) -> C.CDLL:
     if not os.path.exists(path):
         if not build_if_missing:
             raise RuntimeError(f"{path} is missing; run build() first")
@@ -107,6 +125,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     P = C.POINTER(Params)
     vp = C.c_void_p
     dptr = C.POINTER(C.c_double)
+    fptr = C.POINTER(C.c_float)
+    rptr = C.POINTER(real)   # the Fortran build's REAL
     sig = {
         "pcgb_default_params": (None, [P]),
         "pcgb_set_params": (C.c_int, [P]),
@@ -115,20 +135,20 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "pcgb_clear_error": (None, []),
         "pcgb_set_stream": (None, [vp]),
         "pcgb_get_stream": (vp, []),
-        "initializeGPU": (None, [dptr, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "initializeGPU": (None, [rptr, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int]),
         "substepGPU": (None, [C.c_int, C.c_double]),
         "beforeBoundaryGPU": (None, [C.c_bool, C.c_int, C.c_double, C.c_bool]),
         "afterSubStepGPU": (None, []),
         "registerGPU": (None, []),
-        "copyFarray": (None, [dptr]),
+        "copyFarray": (None, [rptr]),
         "loadFarray": (None, []),
         "finalizeGPU": (None, []),
         "reloadConfig": (None, []),
         "prepareForFirstSubstep": (None, [C.c_double]),
-        "getGPUReducedVars": (None, [dptr]),
+        "getGPUReducedVars": (None, [rptr]),
         "copyVBApointers": (None, [C.POINTER(vp), C.POINTER(vp)]),
-        "updateInConfigScalName": (C.c_int, [C.c_char_p, C.c_double]),
-        "updateInConfigVecName": (C.c_int, [C.c_char_p, dptr]),
+        "updateInConfigScalName": (C.c_int, [C.c_char_p, real]),
+        "updateInConfigVecName": (C.c_int, [C.c_char_p, rptr]),
         "testBCs": (None, []),
         "pcgb_get_dt": (C.c_double, []),
         "pcgb_get_time": (C.c_double, []),
@@ -138,6 +158,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "pcgb_box_destroy": (None, [vp]),
         "pcgb_box_load": (C.c_int, [vp, dptr, C.c_double]),
         "pcgb_box_store": (C.c_int, [vp, dptr]),
+        "pcgb_box_load_f32": (C.c_int, [vp, fptr, C.c_double]),
+        "pcgb_box_store_f32": (C.c_int, [vp, fptr]),
         "pcgb_box_init_field": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                           C.c_double, C.c_ulonglong]),
         "pcgb_box_steps": (C.c_int, [vp, C.c_int]),
@@ -170,7 +192,6 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         fn = getattr(L, name)
         fn.restype = res
         fn.argtypes = args
-    _lib = L
     return L
 
 

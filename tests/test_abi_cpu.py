@@ -132,3 +132,39 @@ def test_fortran_module_externals_link(pc):
         r = subprocess.run(["gcc", "-o", os.path.join(d, "f"), c, lib_path, "-Wl,--no-undefined"],
                            capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_single_precision_plugin_library(pc):
+    """libpcgb300_sgl.so, the plug-in for the reference's single-precision build
+    (REAL = float): the same entry points as the double library, the Fortran
+    externals link against it alone, and the header compiles with either REAL."""
+    lib = importlib_lib(pc)
+    S = lib.load_sgl()
+    names = declared_functions()
+    missing = [n for n in names if not hasattr(S, n)]
+    assert not missing, missing
+    assert S._name != pc.load()._name
+    decls = "\n".join(f"extern void {n}_(void);" for n in FORTRAN_EXTERNALS)
+    refs = ", ".join(f"(void*){n}_" for n in FORTRAN_EXTERNALS)
+    prog = f"{decls}\nvoid* table[] = {{{refs}}};\nint main(void) {{ return table[0] == 0; }}\n"
+    inc = os.path.join(os.path.dirname(__file__), "..", "include")
+    hdr = ('#include "pcgb300.h"\n'
+           '_Static_assert(sizeof(REAL_PCGB) == SZ, "REAL");\n'
+           'void (*init)(REAL_PCGB*, int, double, int, int, int, int) = initializeGPU;\n'
+           'void (*copy)(REAL_PCGB*) = copyFarray;\n'
+           'int main(void) { return init == 0 || copy == 0; }\n')
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "f.c")
+        open(c, "w").write(prog)
+        r = subprocess.run(["gcc", "-o", os.path.join(d, "f"), c, S._name, "-Wl,--no-undefined"],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        h = os.path.join(d, "h.c")
+        open(h, "w").write(hdr)
+        for define, size in (("", 8), ("-DPCGB_REAL_SINGLE", 4)):
+            args = ["gcc", "-std=c11", "-I", inc, f"-DSZ={size}", "-o", os.path.join(d, "h"), h,
+                    S._name if define else pc.load()._name, "-Wl,--no-undefined"]
+            if define:
+                args.insert(2, define)
+            r = subprocess.run(args, capture_output=True, text=True)
+            assert r.returncode == 0, (define, r.stderr)
