@@ -176,32 +176,40 @@ __device__ __forceinline__ void add_force(void* f, const HelGeom& g, int target,
 // force goes into aa; uu receives forcing_rhs2 = Re[i coef3 fxyz] with coef3 =
 // crosshel k (k x (k x e)) (:1968, :2276-2281), zero for the default crosshel = 0,
 // so it is not applied.
-// One thread per interior cell: x from blockIdx.x/threadIdx.x, y = blockIdx.y, z = blockIdx.z.
+// One thread per interior (x, y) and a run of kHelZ planes: x from
+// blockIdx.x/threadIdx.x, y = blockIdx.y, planes from blockIdx.z; fx fy is
+// formed once per thread.
+constexpr int kHelZ = 16;
+
 template <int LAYOUT, typename R>
 __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y, k = blockIdx.z;
+  const int j = blockIdx.y;
   if (i >= g.nx) return;
+  const int k0 = blockIdx.z * kHelZ, k1 = min(k0 + kHelZ, g.nz);
   const int target = g.magnetic ? 1 : 0;
   const double* fx = tab + 8;
   const double* fy = fx + 2 * g.nx;
   const double* fz = fy + 2 * g.ny;
   const R xr = (R)fx[2 * i], xi = (R)fx[2 * i + 1];
   const R yr = (R)fy[2 * j], yi = (R)fy[2 * j + 1];
-  const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
   const R pr = rsub(rmul(xr, yr), rmul(xi, yi)), pi = radd(rmul(xr, yi), rmul(xi, yr));   // fx fy
-  const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
-  const CellImages ci(i, j, k, g);
+  const R c1[3] = {(R)tab[0], (R)tab[1], (R)tab[2]}, c2[3] = {(R)tab[3], (R)tab[4], (R)tab[5]};
+#pragma unroll 4
+  for (int k = k0; k < k1; ++k) {
+    const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
+    const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
+    const CellImages ci(i, j, k, g);
 #pragma unroll
-  for (int c = 0; c < 3; ++c)
-    add_force<LAYOUT, R>(f, g, target, c, ci, rsub(rmul((R)tab[c], qr), rmul((R)tab[3 + c], qi)));
+    for (int c = 0; c < 3; ++c) add_force<LAYOUT, R>(f, g, target, c, ci, rsub(rmul(c1[c], qr), rmul(c2[c], qi)));
+  }
 }
 
 cudaError_t launch_helical(int layout, void* f, const HelRec* ring, const PcgbBoxState* state, double* tab,
                            const HelGeom& g, cudaStream_t s) {
   if (g.ny > 65535 || g.nz > 65535) return cudaErrorInvalidValue;   // grid y/z limits
   helical_tables_kernel<<<1, 256, 0, s>>>(ring, state, tab, g);
-  const dim3 grid((unsigned)((g.nx + 127) / 128), (unsigned)g.ny, (unsigned)g.nz);
+  const dim3 grid((unsigned)((g.nx + 127) / 128), (unsigned)g.ny, (unsigned)((g.nz + kHelZ - 1) / kHelZ));
   switch (layout) {
     case HEL_F32: helical_apply_kernel<HEL_F32, float><<<grid, 128, 0, s>>>(f, tab, g); break;
     case HEL_F64: helical_apply_kernel<HEL_F64, double><<<grid, 128, 0, s>>>(f, tab, g); break;

@@ -22,6 +22,7 @@ MODES = {
     "f64": dict(precision=8),
     "f64_tile1": dict(precision=8, tile=1),
     "dfloat": dict(precision=8, dfloat=1, tile=3),
+    "dfloat_tile2": dict(precision=8, dfloat=1, tile=2),
     "dfloat_pair": dict(precision=8, dfloat=1),
     "dfloat_pair6": dict(precision=8, dfloat=1, tile=6),
     "f32pair": dict(precision=4, comp=1),
@@ -190,3 +191,27 @@ def test_upwinding_through_noalloc_entry(pc, ic, orc):
     g = from_device_layout(bufs[1].cpu().numpy(), xoff, p.nx + 6)
     ref, _ = _oracle(orc, p, f0, 1)
     _check(g, ref, p, "f64")
+
+
+@pytest.mark.parametrize("prec", [4, 8])
+def test_upwinding_batch_equals_single(pc, ic, prec):
+    """Boxes with upwinding in one persistent batched launch give each box's result alone."""
+    sizes = [(24, 20, 16), (16, 16, 16), (32, 24, 8)]
+    kw = dict(precision=prec, comp=1) if prec == 4 else dict(precision=8)
+    alone, boxes = [], []
+    for i, n in enumerate(sizes):
+        p = _params(pc, n=n, nu=2e-3 * (i + 1), **kw)
+        f0 = _initial(pc, ic, p, seed=30 + i)
+        b = pc.Box(p)
+        b.load(f0)
+        b.steps(4)
+        alone.append(b.store())
+        b.close()
+        b = pc.Box(p)
+        b.load(f0)
+        boxes.append(b)
+    batch = pc.Batch(boxes)
+    batch.steps(4, use_graph=True, graph_steps=2)
+    for b, ref in zip(boxes, alone):
+        assert np.array_equal(b.store(), ref)
+    batch.close()
