@@ -131,36 +131,57 @@ struct CellImages {
   }
 };
 
-// Component c of uu (target 0) or aa (target 1): the value at the interior
-// cell plus v, stored there and at the cell's periodic ghost images (copies of
-// the interior value after a substep).  Pair layouts move whole elements; only
-// the target lane changes.
+// Element access of one layout: the element type E, the slice of component c
+// of uu (target 0) or aa (target 1), and the element with v added to the
+// target value.  Pair layouts move whole elements; only the target lane changes.
 template <int LAYOUT, typename R>
-__device__ __forceinline__ void add_force(void* f, const HelGeom& g, int target, int c, const CellImages& ci, R v) {
-  const long long cell = ci.at(0, 0, 0);
-  if (LAYOUT == HEL_F32 || LAYOUT == HEL_F64 || LAYOUT == HEL_DD) {
-    const long long base = (long long)(target ? g.iax + c : c) * g.fs;   // field-major slice
-    if (LAYOUT == HEL_F32) {
-      float* p = static_cast<float*>(f) + base;
-      ci.store(p, radd(p[cell], (float)v));
-    } else if (LAYOUT == HEL_F64) {
-      double* p = static_cast<double*>(f) + base;
-      ci.store(p, radd(p[cell], (double)v));
-    } else {
-      float2* p = static_cast<float2*>(f) + base;   // (hi, lo)
-      const float2 e = p[cell];
-      const dd w(__dadd_rn((double)e.x + (double)e.y, (double)v));
-      ci.store(p, make_float2(w.hi, w.lo));
-    }
-  } else if (LAYOUT == HEL_F32_PAIR) {
-    float2* p = static_cast<float2*>(f) + (long long)c * g.fs;   // pair (u_c, A_c)
-    float2 e = p[cell];
+struct HelElem;
+template <typename R>
+struct HelElem<HEL_F32, R> {
+  using E = float;
+  static __device__ __forceinline__ E* slice(void* f, const HelGeom& g, int target, int c) {
+    return static_cast<E*>(f) + (long long)(target ? g.iax + c : c) * g.fs;
+  }
+  static __device__ __forceinline__ E add(E e, int, R v) { return radd(e, (float)v); }
+};
+template <typename R>
+struct HelElem<HEL_F64, R> {
+  using E = double;
+  static __device__ __forceinline__ E* slice(void* f, const HelGeom& g, int target, int c) {
+    return static_cast<E*>(f) + (long long)(target ? g.iax + c : c) * g.fs;
+  }
+  static __device__ __forceinline__ E add(E e, int, R v) { return radd(e, (double)v); }
+};
+template <typename R>
+struct HelElem<HEL_DD, R> {
+  using E = float2;   // (hi, lo)
+  static __device__ __forceinline__ E* slice(void* f, const HelGeom& g, int target, int c) {
+    return static_cast<E*>(f) + (long long)(target ? g.iax + c : c) * g.fs;
+  }
+  static __device__ __forceinline__ E add(E e, int, R v) {
+    const dd w(__dadd_rn((double)e.x + (double)e.y, (double)v));
+    return make_float2(w.hi, w.lo);
+  }
+};
+template <typename R>
+struct HelElem<HEL_F32_PAIR, R> {
+  using E = float2;   // pair (u_c, A_c)
+  static __device__ __forceinline__ E* slice(void* f, const HelGeom& g, int, int c) {
+    return static_cast<E*>(f) + (long long)c * g.fs;
+  }
+  static __device__ __forceinline__ E add(E e, int target, R v) {
     if (target) e.y = radd(e.y, (float)v);
     else e.x = radd(e.x, (float)v);
-    ci.store(p, e);
-  } else {
-    float4* p = static_cast<float4*>(f) + (long long)c * g.fs;   // dd2: (hi.x, hi.y, lo.x, lo.y)
-    float4 e = p[cell];
+    return e;
+  }
+};
+template <typename R>
+struct HelElem<HEL_DD_PAIR, R> {
+  using E = float4;   // dd2: (hi.x, hi.y, lo.x, lo.y)
+  static __device__ __forceinline__ E* slice(void* f, const HelGeom& g, int, int c) {
+    return static_cast<E*>(f) + (long long)c * g.fs;
+  }
+  static __device__ __forceinline__ E add(E e, int target, R v) {
     if (target) {
       const dd w(__dadd_rn((double)e.y + (double)e.w, (double)v));
       e.y = w.hi; e.w = w.lo;
@@ -168,9 +189,9 @@ __device__ __forceinline__ void add_force(void* f, const HelGeom& g, int target,
       const dd w(__dadd_rn((double)e.x + (double)e.z, (double)v));
       e.x = w.hi; e.z = w.lo;
     }
-    ci.store(p, e);
+    return e;
   }
-}
+};
 
 // forcing_hel with lmagnetic_forcing (forcing.f90:318-345, :2289-2311): the
 // force goes into aa; uu receives forcing_rhs2 = Re[i coef3 fxyz] with coef3 =
@@ -178,11 +199,17 @@ __device__ __forceinline__ void add_force(void* f, const HelGeom& g, int target,
 // so it is not applied.
 // One thread per interior (x, y) and a run of kHelZ planes: x from
 // blockIdx.x/threadIdx.x, y = blockIdx.y, planes from blockIdx.z; fx fy is
-// formed once per thread.
-constexpr int kHelZ = 16;
+// formed once per thread.  The forced components of kHelB planes are loaded
+// before any is stored (the stores could alias the loads as far as the
+// compiler knows), which keeps 3 kHelB loads in flight per thread.  Each value
+// is stored at the interior cell and at its periodic ghost images (copies of
+// the interior value after a substep).
+constexpr int kHelZ = 16, kHelB = 4;
 
 template <int LAYOUT, typename R>
 __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
+  using A = HelElem<LAYOUT, R>;
+  using E = typename A::E;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= g.nx) return;
@@ -195,13 +222,30 @@ __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
   const R yr = (R)fy[2 * j], yi = (R)fy[2 * j + 1];
   const R pr = rsub(rmul(xr, yr), rmul(xi, yi)), pi = radd(rmul(xr, yi), rmul(xi, yr));   // fx fy
   const R c1[3] = {(R)tab[0], (R)tab[1], (R)tab[2]}, c2[3] = {(R)tab[3], (R)tab[4], (R)tab[5]};
-#pragma unroll 4
-  for (int k = k0; k < k1; ++k) {
-    const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
-    const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
-    const CellImages ci(i, j, k, g);
+  E* sl[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) add_force<LAYOUT, R>(f, g, target, c, ci, rsub(rmul(c1[c], qr), rmul(c2[c], qi)));
+  for (int c = 0; c < 3; ++c) sl[c] = A::slice(f, g, target, c);
+  for (int kb = k0; kb < k1; kb += kHelB) {
+    E e[kHelB][3];
+#pragma unroll
+    for (int u = 0; u < kHelB; ++u) {
+      if (kb + u < k1) {
+        const long long cell = (long long)(kb + u + 3) * g.ps + (long long)(j + 3) * g.px + g.xoff + i;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) e[u][c] = sl[c][cell];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kHelB; ++u) {
+      if (kb + u < k1) {
+        const int k = kb + u;
+        const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
+        const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
+        const CellImages ci(i, j, k, g);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ci.store(sl[c], A::add(e[u][c], target, rsub(rmul(c1[c], qr), rmul(c2[c], qi))));
+      }
+    }
   }
 }
 
