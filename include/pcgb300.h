@@ -85,7 +85,18 @@ typedef struct pcgb_params {
                               into aa; each step also draws the secondary record of lmhd_forcing, whose
                               force on uu is zero for crosshel = 0 (forcing.f90:314-345, :2136-2311) */
   int pad_;                /* keeps the struct a multiple of 8 bytes; set to 0 */
+  int bc[3][8][2];         /* boundary condition of direction x/y/z, field (f-array order), side
+                              (0 lower, 1 upper): PCGB_BC_* codes (&init_pars bcx/bcy/bcz,
+                              boundcond.f90); all 0 = periodic.  A direction is periodic when every
+                              code is PCGB_BC_PER and non-periodic when none is; its grid then has
+                              points on both boundaries, dx = L/(n-1) (grid.f90:123-151) */
 } pcgb_params;
+
+/* Boundary condition codes (boundcond.f90 bcx/bcy/bcz, bc_sym_x/y/z:2637,3483,3842). */
+#define PCGB_BC_PER 0    /* 'p'  periodic */
+#define PCGB_BC_SYM 1    /* 's'  f(n1-i) = f(n1+i) */
+#define PCGB_BC_ASYM 2   /* 'a'  f(n1-i) = -f(n1+i), f(n1) = 0 */
+#define PCGB_BC_ASYM2 3  /* 'a2' f(n1-i) = 2 f(n1) - f(n1+i) */
 
 /* Defaults of the reference (cdata.f90:211,235,239; eos_idealgas.f90:47;
    forcing.f90:37,129; hydro.f90:283; magnetic.f90:247; entropy.f90:139). */

@@ -38,6 +38,7 @@ class OrcParams(C.Structure):
         ("lohmic_heat", C.c_int), ("lviscosity_heat", C.c_int),
         ("cdt", C.c_double), ("cdtv", C.c_double),
         ("lupw_uu", C.c_int), ("lupw_lnrho", C.c_int),
+        ("bc", ((C.c_int * 2) * 8) * 3),
     ]
 
 
@@ -71,7 +72,7 @@ def lib():
         dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="F_CONTIGUOUS")
         dpc = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
         P = C.POINTER(OrcParams)
-        L.orc_ghosts_periodic.argtypes = [P, dp, C.c_int]
+        L.orc_boundconds.argtypes = [P, dp, C.c_int]
         L.orc_stencil_field.argtypes = [P, dp, C.c_int, C.c_int, C.c_int, C.c_int, dp]
         L.orc_pde.argtypes = [P, dp, dp, C.c_double, C.c_int, C.POINTER(C.c_double), C.c_void_p, C.c_int]
         L.orc_time_step.argtypes = [P, dp, dp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
@@ -102,6 +103,10 @@ def make_params(**kw) -> OrcParams:
     for k, v in d.items():
         if k == "b_ext":
             p.b_ext[:] = list(v)
+        elif k == "bc":
+            for a in range(3):
+                for f in range(8):
+                    p.bc[a][f][0], p.bc[a][f][1] = v[a][f][0], v[a][f][1]
         else:
             setattr(p, k, v)
     return p
@@ -123,7 +128,7 @@ def grid(p: OrcParams):
 
 
 def ghosts(p: OrcParams, f: np.ndarray) -> None:
-    lib().orc_ghosts_periodic(C.byref(p), f, f.shape[3])
+    lib().orc_boundconds(C.byref(p), f, f.shape[3])
 
 
 def stencil(p: OrcParams, f: np.ndarray, k: int, kind: int, i: int, j: int = 0) -> np.ndarray:

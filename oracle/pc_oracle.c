@@ -39,13 +39,29 @@ static inline size_t IDX(const ctx_t* c, int l, int m, int n, int k) {
 
 int orc_nfields(const orc_params* p) { return p->lentropy ? 8 : 7; }
 
-/* Equidistant periodic cell-centred grid, src/grid.f90:123-151:
-   dx = Lx/nx, x(i) = x0 + (i - nghost - 1 + 1/2) dx  (1-based i). */
+/* A direction is periodic when every field's code on both sides is 'p'. */
+static int orc_periodic(const orc_params* p, int d) {
+  for (int k = 0; k < orc_nfields(p); ++k)
+    if (p->bc[d][k][0] != ORC_BC_PER || p->bc[d][k][1] != ORC_BC_PER) return 0;
+  return 1;
+}
+
+/* Equidistant grid, src/grid.f90:123-151: on a periodic axis dx = Lx/nx and
+   x(i) = x0 + (i - nghost - 1 + 1/2) dx (1-based i, cell centres); otherwise
+   dx = Lx/(nx-1) and x(i) = x0 + (i - nghost - 1) dx (points on both boundaries). */
+static double orc_spacing(const orc_params* p, int d) {
+  const int n = d == 0 ? p->nx : d == 1 ? p->ny : p->nz;
+  const double L = d == 0 ? p->Lx : d == 1 ? p->Ly : p->Lz;
+  return L / (orc_periodic(p, d) ? n : n - 1);
+}
+
 void orc_grid(const orc_params* p, double* x, double* y, double* z) {
-  double dx = p->Lx / p->nx, dy = p->Ly / p->ny, dz = p->Lz / p->nz;
-  for (int i = 0; i < p->nx + 2 * NG; ++i) x[i] = p->x0 + ((double)(i - NG) + 0.5) * dx;
-  for (int i = 0; i < p->ny + 2 * NG; ++i) y[i] = p->y0 + ((double)(i - NG) + 0.5) * dy;
-  for (int i = 0; i < p->nz + 2 * NG; ++i) z[i] = p->z0 + ((double)(i - NG) + 0.5) * dz;
+  const double dx = orc_spacing(p, 0), dy = orc_spacing(p, 1), dz = orc_spacing(p, 2);
+  const double ox = orc_periodic(p, 0) ? 0.5 : 0.0, oy = orc_periodic(p, 1) ? 0.5 : 0.0,
+               oz = orc_periodic(p, 2) ? 0.5 : 0.0;
+  for (int i = 0; i < p->nx + 2 * NG; ++i) x[i] = p->x0 + ((double)(i - NG) + ox) * dx;
+  for (int i = 0; i < p->ny + 2 * NG; ++i) y[i] = p->y0 + ((double)(i - NG) + oy) * dy;
+  for (int i = 0; i < p->nz + 2 * NG; ++i) z[i] = p->z0 + ((double)(i - NG) + oz) * dz;
 }
 
 static void ctx_init(ctx_t* c, const orc_params* p) {
@@ -55,9 +71,9 @@ static void ctx_init(ctx_t* c, const orc_params* p) {
   c->iux = 0; c->iuy = 1; c->iuz = 2; c->ilnrho = 3;
   if (p->lentropy) { c->iss = 4; c->iax = 5; } else { c->iss = -1; c->iax = 4; }
   c->iay = c->iax + 1; c->iaz = c->iax + 2;
-  c->dx_1 = 1.0 / (p->Lx / p->nx);
-  c->dy_1 = 1.0 / (p->Ly / p->ny);
-  c->dz_1 = 1.0 / (p->Lz / p->nz);
+  c->dx_1 = 1.0 / orc_spacing(p, 0);
+  c->dy_1 = 1.0 / orc_spacing(p, 1);
+  c->dz_1 = 1.0 / orc_spacing(p, 2);
   /* dxyz_2 = dline_1(:,1)**2 + dline_1(:,2)**2 + dline_1(:,3)**2, grid.f90:3051 */
   c->dxyz_2 = (c->dx_1 * c->dx_1 + c->dy_1 * c->dy_1) + c->dz_1 * c->dz_1;
   /* units_eos, eos_idealgas.f90:158-268 */
@@ -94,32 +110,56 @@ static void ctx_free(ctx_t* c) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* Periodic ghosts: bc_per_x (boundcond.f90:2387), bc_per_y (:2411),
-   bc_per_z (:2509), applied x, then y, then z over the full extent of the
-   other axes so that edges and corners are consistent. */
-void orc_ghosts_periodic(const orc_params* p, double* f, int nf) {
+/* One field's ghosts on one side of direction d, over the full extent of the
+   other two axes: bc_per_x/y/z (boundcond.f90:2387-2531) for 'p', bc_sym_x/y/z
+   (:2637-2677, :3483-3530, :3842-3900) for 's' (sgn +1), 'a' (sgn -1, boundary
+   value set to 0) and 'a2' (sgn -1, REL). */
+static void bc_side(const orc_params* p, const ctx_t* c, double* f, int k, int d, int side) {
+  const int code = p->bc[d][k][side];
+  const int n = d == 0 ? p->nx : d == 1 ? p->ny : p->nz;
+  const int na = d == 0 ? c->my : c->mx, nb = d == 0 ? c->mz : (d == 1 ? c->mz : c->my);
+  const size_t st = d == 0 ? 1 : d == 1 ? (size_t)c->mx : (size_t)c->mx * c->my;
+  const int b1 = NG, b2 = NG + n - 1;   /* n1, n2 (0-based array indices) */
+  for (int ib = 0; ib < nb; ++ib)
+    for (int ia = 0; ia < na; ++ia) {
+      size_t base;   /* element at index 0 along d */
+      if (d == 0) base = IDX(c, 0, ia, ib, k);
+      else if (d == 1) base = IDX(c, ia, 0, ib, k);
+      else base = IDX(c, ia, ib, 0, k);
+      double* q = f + base;
+      if (code == ORC_BC_PER) {
+        for (int i = 1; i <= NG; ++i) {
+          if (side == 0) q[(size_t)(b1 - i) * st] = q[(size_t)(b2 + 1 - i) * st];   /* f(n1-i) = f(n2+1-i) */
+          else q[(size_t)(b2 + i) * st] = q[(size_t)(b1 - 1 + i) * st];              /* f(n2+i) = f(n1-1+i) */
+        }
+        continue;
+      }
+      const double sgn = (code == ORC_BC_SYM) ? 1.0 : -1.0;
+      if (side == 0) {
+        for (int i = 1; i <= NG; ++i) {
+          const double fi = q[(size_t)(b1 + i) * st], f0 = q[(size_t)b1 * st];
+          q[(size_t)(b1 - i) * st] = (code == ORC_BC_ASYM2) ? 2.0 * f0 + sgn * fi : sgn * fi;
+        }
+        if (code == ORC_BC_ASYM) q[(size_t)b1 * st] = 0.0;
+      } else {
+        for (int i = 1; i <= NG; ++i) {
+          const double fi = q[(size_t)(b2 - i) * st], f0 = q[(size_t)b2 * st];
+          double g;
+          if (code != ORC_BC_ASYM2) g = sgn * fi;
+          else if (d == 2) g = f0 + (f0 + sgn * fi);   /* bc_sym_z top, :3886 */
+          else g = 2.0 * f0 + sgn * fi;
+          q[(size_t)(b2 + i) * st] = g;
+        }
+        if (code == ORC_BC_ASYM) q[(size_t)b2 * st] = 0.0;
+      }
+    }
+}
+
+void orc_boundconds(const orc_params* p, double* f, int nf) {
   ctx_t c; ctx_init(&c, p);
-  int nx = p->nx, ny = p->ny, nz = p->nz;
-  for (int k = 0; k < nf; ++k) {
-    for (int n = NG; n < NG + nz; ++n)
-      for (int m = NG; m < NG + ny; ++m)
-        for (int g = 0; g < NG; ++g) {
-          f[IDX(&c, g, m, n, k)] = f[IDX(&c, g + nx, m, n, k)];
-          f[IDX(&c, NG + nx + g, m, n, k)] = f[IDX(&c, NG + g, m, n, k)];
-        }
-    for (int n = NG; n < NG + nz; ++n)
-      for (int g = 0; g < NG; ++g)
-        for (int l = 0; l < c.mx; ++l) {
-          f[IDX(&c, l, g, n, k)] = f[IDX(&c, l, g + ny, n, k)];
-          f[IDX(&c, l, NG + ny + g, n, k)] = f[IDX(&c, l, NG + g, n, k)];
-        }
-    for (int g = 0; g < NG; ++g)
-      for (int m = 0; m < c.my; ++m)
-        for (int l = 0; l < c.mx; ++l) {
-          f[IDX(&c, l, m, g, k)] = f[IDX(&c, l, m, g + nz, k)];
-          f[IDX(&c, l, m, NG + nz + g, k)] = f[IDX(&c, l, m, NG + g, k)];
-        }
-  }
+  for (int d = 0; d < 3; ++d)          /* boundconds_x, then _y, then _z */
+    for (int k = 0; k < nf; ++k)
+      for (int side = 0; side < 2; ++side) bc_side(p, &c, f, k, d, side);
   ctx_free(&c);
 }
 
@@ -462,7 +502,7 @@ void orc_time_step(const orc_params* p, double* f, double* df, double* t, double
   for (int itsub = 0; itsub < 3; ++itsub) {
     double alpha = alpha_ts[itsub];
     if (itsub == 0) ds = 0.0; else ds = alpha * ds;
-    orc_ghosts_periodic(p, f, nf);
+    orc_boundconds(p, f, nf);
     double dt1 = 0.0;
     /* substep 1 with df = 0 (alpha = 0 makes alpha*df = 0 for finite df) */
     if (itsub == 0) {

@@ -33,7 +33,11 @@ typedef struct {
   int lohmic_heat, lviscosity_heat;
   double cdt, cdtv;
   int lupw_uu, lupw_lnrho;  /* upwinded advection (hydro.f90:3662, density.f90:2772) */
+  int bc[3][8][2];          /* boundary condition of direction, field, side (0 lower, 1 upper):
+                               0 'p', 1 's', 2 'a', 3 'a2' (boundcond.f90); all 0 = periodic */
 } orc_params;
+
+enum { ORC_BC_PER = 0, ORC_BC_SYM = 1, ORC_BC_ASYM = 2, ORC_BC_ASYM2 = 3 };
 
 /* Diagnostic slots (FP64), evaluated on f at the start of a step. */
 enum {
@@ -45,7 +49,10 @@ int  orc_nfields(const orc_params* p);
 void orc_grid(const orc_params* p, double* x, double* y, double* z);
 
 /* Periodic ghost filling, x then y then z (src/boundcond.f90:2387-2531). */
-void orc_ghosts_periodic(const orc_params* p, double* f, int nf);
+/* Ghost zones as pde sets them before the RHS (equ.f90: boundconds_x, _y, _z),
+   with bc_per_x/y/z (boundcond.f90:2387-2531) and bc_sym_x/y/z (:2637-2677,
+   :3483-3530, :3842-3900) per field and side. */
+void orc_boundconds(const orc_params* p, double* f, int nf);
 
 /* Stencils on a single interior point (0-based ghosted indices l,m,n),
    field k, direction j (0,1,2).  deriv.f90:89 / :472 / :1367. */

@@ -79,7 +79,7 @@ __global__ void load_rows_kernel(T* __restrict__ f, const H* __restrict__ stage,
 template <typename T, typename H>
 __global__ void store_rows_kernel(H* __restrict__ stage, const T* __restrict__ f, const T* __restrict__ carry,
                                   long long r0, long long nr, int nx, int ny, int nz, int px, int my, int mz,
-                                  int xoff, int nf, int pairs) {
+                                  int xoff, int nf, int pairs, int permask) {
   const int mx = nx + 6;
   const long long total = nr * mx;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
@@ -93,8 +93,11 @@ __global__ void store_rows_kernel(H* __restrict__ stage, const T* __restrict__ f
       long long rr = row / my;
       const int k = (int)(rr % mz);
       const long long fld = rr / mz;
+      // a ghost of a non-periodic axis (bit clear in permask) holds its boundary value alone
+      const bool bghost = (!(permask & 1) && (i < 3 || i >= nx + 3)) || (!(permask & 2) && (j < 3 || j >= ny + 3)) ||
+                          (!(permask & 4) && (k < 3 || k >= nz + 3));
       const long long crow = (long long)(wrap(j, ny) + 3) + (long long)my * ((wrap(k, nz) + 3) + (long long)mz * fld);
-      v += (double)carry[dev_index(crow, wrap(i, nx) + 3, my, mz, px, xoff, nf, pairs)];
+      if (!bghost) v += (double)carry[dev_index(crow, wrap(i, nx) + 3, my, mz, px, xoff, nf, pairs)];
     }
     stage[q] = (H)v;
   }
@@ -176,28 +179,29 @@ cudaError_t launch_load_rows(int tbytes, int hbytes, void* f, const void* stage,
 
 template <typename H>
 static void store_rows(int tbytes, H* stage, const void* f, const void* carry, long long r0, long long nr, int nx,
-                       int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs, cudaStream_t s) {
+                       int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs, int permask,
+                       cudaStream_t s) {
   const int th = 256, g = grid_for(nr * (nx + 6), th);
   if (tbytes == 4)
     store_rows_kernel<float, H><<<g, th, 0, s>>>(stage, (const float*)f, (const float*)carry, r0, nr, nx, ny, nz, px,
-                                                 my, mz, xoff, nf, pairs);
+                                                 my, mz, xoff, nf, pairs, permask);
   else if (tbytes == kElemDD)
     store_rows_kernel<dd, H><<<g, th, 0, s>>>(stage, (const dd*)f, nullptr, r0, nr, nx, ny, nz, px, my, mz, xoff, nf,
-                                              pairs);
+                                              pairs, permask);
   else if (tbytes == kElemDDPair)
     store_rows_ddpair_kernel<H><<<g, th, 0, s>>>(stage, (const float*)f, r0, nr, nx, my, mz, px, xoff, nf);
   else
     store_rows_kernel<double, H><<<g, th, 0, s>>>(stage, (const double*)f, (const double*)carry, r0, nr, nx, ny, nz,
-                                                  px, my, mz, xoff, nf, pairs);
+                                                  px, my, mz, xoff, nf, pairs, permask);
 }
 
 cudaError_t launch_store_rows(int tbytes, int hbytes, void* stage, const void* f, const void* carry, long long r0,
                               long long nr, int nx, int ny, int nz, int px, int my, int mz, int xoff, int nf, int pairs,
-                              cudaStream_t s) {
+                              int permask, cudaStream_t s) {
   if (hbytes == 4)
-    store_rows(tbytes, (float*)stage, f, carry, r0, nr, nx, ny, nz, px, my, mz, xoff, nf, pairs, s);
+    store_rows(tbytes, (float*)stage, f, carry, r0, nr, nx, ny, nz, px, my, mz, xoff, nf, pairs, permask, s);
   else
-    store_rows(tbytes, (double*)stage, f, carry, r0, nr, nx, ny, nz, px, my, mz, xoff, nf, pairs, s);
+    store_rows(tbytes, (double*)stage, f, carry, r0, nr, nx, ny, nz, px, my, mz, xoff, nf, pairs, permask, s);
   return cudaGetLastError();
 }
 
@@ -240,7 +244,8 @@ struct DDPairRef {
 template <class REF>
 __global__ void init_field_kernel(REF f, int kind, int comp, double ampl, double a, double b, double c, double k,
                                   unsigned long long seed, int nx, int ny, int nz, int px, int my, int xoff, double x0,
-                                  double y0, double z0, double dx, double dy, double dz) {
+                                  double y0, double z0, double dx, double dy, double dz, double ox, double oy,
+                                  double oz) {
   const long long total = (long long)nx * ny * nz;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
@@ -259,7 +264,8 @@ __global__ void init_field_kernel(REF f, int kind, int comp, double ampl, double
       const double g = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
       f.set(idx, f.get(idx) + ampl * g);
     } else {
-      const double x = x0 + ((double)i + 0.5) * dx, y = y0 + ((double)j + 0.5) * dy, z = z0 + ((double)kk + 0.5) * dz;
+      // grid point i of an axis: x0 + (i + o) dx, o = 1/2 on a periodic axis, 0 otherwise
+      const double x = x0 + ((double)i + ox) * dx, y = y0 + ((double)j + oy) * dy, z = z0 + ((double)kk + oz) * dz;
       double v;
       if (comp == 0) v = a * sin(k * z) + c * cos(k * y);
       else if (comp == 1) v = b * sin(k * x) + a * cos(k * z);
@@ -271,21 +277,22 @@ __global__ void init_field_kernel(REF f, int kind, int comp, double ampl, double
 
 cudaError_t launch_init_field(int tbytes, void* f, int kind, int comp, double ampl, double a, double b, double c,
                               double k, unsigned long long seed, int nx, int ny, int nz, int px, int my, int xoff,
-                              double x0, double y0, double z0, double dx, double dy, double dz, int estride,
+                              double x0, double y0, double z0, double dx, double dy, double dz, double ox, double oy,
+                              double oz, int estride,
                               cudaStream_t s) {
   const int th = 256, g = grid_for((long long)nx * ny * nz, th);
   if (tbytes == 4)
     init_field_kernel<<<g, th, 0, s>>>(ElemRef<float>{(float*)f, estride}, kind, comp, ampl, a, b, c, k, seed, nx, ny,
-                                       nz, px, my, xoff, x0, y0, z0, dx, dy, dz);
+                                       nz, px, my, xoff, x0, y0, z0, dx, dy, dz, ox, oy, oz);
   else if (tbytes == kElemDD)
     init_field_kernel<<<g, th, 0, s>>>(ElemRef<dd>{(dd*)f, estride}, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz,
-                                       px, my, xoff, x0, y0, z0, dx, dy, dz);
+                                       px, my, xoff, x0, y0, z0, dx, dy, dz, ox, oy, oz);
   else if (tbytes == kElemDDPair)
     init_field_kernel<<<g, th, 0, s>>>(DDPairRef{(float*)f}, kind, comp, ampl, a, b, c, k, seed, nx, ny, nz, px, my,
-                                       xoff, x0, y0, z0, dx, dy, dz);
+                                       xoff, x0, y0, z0, dx, dy, dz, ox, oy, oz);
   else
     init_field_kernel<<<g, th, 0, s>>>(ElemRef<double>{(double*)f, estride}, kind, comp, ampl, a, b, c, k, seed, nx,
-                                       ny, nz, px, my, xoff, x0, y0, z0, dx, dy, dz);
+                                       ny, nz, px, my, xoff, x0, y0, z0, dx, dy, dz, ox, oy, oz);
   return cudaGetLastError();
 }
 

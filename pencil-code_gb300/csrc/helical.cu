@@ -81,19 +81,19 @@ __global__ void helical_tables_kernel(const HelRec* ring, const PcgbBoxState* S,
   double* fz = fy + 2 * g.ny;
   for (int i = threadIdx.x; i < g.nx + g.ny + g.nz; i += blockDim.x) {
     if (i < g.nx) {
-      const double x = __dadd_rn(g.x0, __dmul_rn((double)i + 0.5, g.dx));
+      const double x = __dadd_rn(g.x0, __dmul_rn((double)i + g.ox, g.dx));
       const double a = __dadd_rn(__dmul_rn(__dmul_rn(r.kk[0], g.k1), x), r.phase);
       fx[2 * i] = __dmul_rn(cos(a), fact);
       fx[2 * i + 1] = __dmul_rn(sin(a), fact);
     } else if (i < g.nx + g.ny) {
       const int j = i - g.nx;
-      const double y = __dadd_rn(g.y0, __dmul_rn((double)j + 0.5, g.dy));
+      const double y = __dadd_rn(g.y0, __dmul_rn((double)j + g.oy, g.dy));
       const double a = __dmul_rn(__dmul_rn(r.kk[1], g.k1), y);
       fy[2 * j] = cos(a);
       fy[2 * j + 1] = sin(a);
     } else {
       const int k = i - g.nx - g.ny;
-      const double z = __dadd_rn(g.z0, __dmul_rn((double)k + 0.5, g.dz));
+      const double z = __dadd_rn(g.z0, __dmul_rn((double)k + g.oz, g.dz));
       const double a = __dmul_rn(__dmul_rn(r.kk[2], g.k1), z);
       fz[2 * k] = cos(a);
       fz[2 * k + 1] = sin(a);

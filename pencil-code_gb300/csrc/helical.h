@@ -27,6 +27,7 @@ struct HelGeom {
   int nx, ny, nz, px, my, xoff;
   long long ps, fs;   // plane and slice strides in elements
   double x0, y0, z0, dx, dy, dz, k1;
+  double ox, oy, oz;  // grid point i of an axis is x0 + (i + o) dx: o = 1/2 periodic, 0 otherwise
   int iax;            // first slice of aa (field-major layouts)
   int magnetic;       // 1: the force goes into aa (lmagnetic_forcing), 0: into uu
 };

@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include "boundcond.h"
 #include "../../include/pcgb300.h"
 #include "kernels.cuh"
 #include "pcgb_box.h"
@@ -67,6 +68,8 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
   if (p->precision != 4 && p->precision != 8) return fail(2, "precision must be 4 or 8");
   if (p->dfloat) return fail(2, "double-float state is not available here (use the box API)");
   if (p->lforcing_hel) return fail(2, "the step-end helical forcing is applied by the box API only");
+  for (int d = 0; d < 3; ++d)
+    if (!axis_periodic(*p, d)) return fail(2, "non-periodic boundaries are applied by the box API only");
   if (p->nx < 6 || p->ny < 6 || p->nz < 6 || p->nx > kMaxExtent || p->ny > kMaxExtent || p->nz > kMaxExtent)
     return fail(7, "grid extent outside [6, PCGB_NOALLOC_MAX_EXTENT]");
   cudaStream_t s = static_cast<cudaStream_t>(stream);

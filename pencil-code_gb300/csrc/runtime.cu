@@ -26,6 +26,7 @@
 
 #include "../../include/pcgb300.h"
 #include "aux_kernels.h"
+#include "boundcond.h"
 #include "cfl_pair.h"
 #include "helical.h"
 #include "kernels.cuh"
@@ -150,6 +151,7 @@ struct pcgb_box {
   int tiles = 0;
   unsigned long long nsub = 0;  // host mirror of the device substep counter
   bool dt_known = false;
+  bool nonper = false;   // some direction has non-periodic boundary conditions
   bool diag_pending = false;    // a diagnostics request not yet served by a substep-1 launch
   KernelHandle kh;
   // random helical forcing: wavevector list (kkx, kky, kkz), its mean |k|, the
@@ -167,10 +169,28 @@ struct pcgb_box {
 // Element code of the layout kernels: float, double or double-float.
 static int elem_code(const pcgb_box* b) { return b->dfl ? (b->pairs ? kElemDDPair : kElemDD) : b->tb; }
 
+// Element layout code of the helical forcing and boundary kernels (HelLayout).
+static int hel_layout(const pcgb_box* b) {
+  if (b->tb == 4) return b->pairs ? HEL_F32_PAIR : HEL_F32;
+  if (b->dfl) return b->pairs ? HEL_DD_PAIR : HEL_DD;
+  return HEL_F64;
+}
+
+// Ghost zones of the non-periodic directions of the current f (boundconds_x/y/z
+// at the start of pde, equ.f90; update_ghosts before a snapshot).
+static int box_boundconds(pcgb_box* b) {
+  // the FP32 carry lives in df between steps (substep counter at a step boundary)
+  void* carry = (b->hdev.comp && (b->nsub % 3) == 0) ? b->df : nullptr;
+  CK(launch_boundconds(hel_layout(b), b->f[b->nsub & 1ull], carry, b->p, b->nx, b->ny, b->nz, b->px, b->my, b->mz,
+                       b->xoff, b->ps, b->fs, b->nf, g.stream));
+  g.launches += !axis_periodic(b->p, 0) + !axis_periodic(b->p, 1) + !axis_periodic(b->p, 2);
+  return 0;
+}
+
 static void fill_physics(pcgb_box* b) {
   const pcgb_params& p = b->p;
   PcgbBoxDev& d = b->hdev;
-  const double dx = p.Lxyz[0] / p.nx, dy = p.Lxyz[1] / p.ny, dz = p.Lxyz[2] / p.nz;
+  const double dx = axis_spacing(p, 0), dy = axis_spacing(p, 1), dz = axis_spacing(p, 2);
   d.dx_1 = 1.0 / dx; d.dy_1 = 1.0 / dy; d.dz_1 = 1.0 / dz;
   d.dxyz_2 = (d.dx_1 * d.dx_1 + d.dy_1 * d.dy_1) + d.dz_1 * d.dz_1;   // grid.f90:3051
   d.nu = p.nu; d.eta = p.eta; d.chi = p.chi; d.mu0 = p.mu0; d.mu01 = 1.0 / p.mu0;
@@ -198,17 +218,18 @@ static void fill_physics(pcgb_box* b) {
 }
 
 // ABC forcing tables sin/cos(kf*x) over the ghosted grid, forcing.f90:1100-1104,
-// grid x_i = x0 + (i - 3 + 1/2) dx (grid.f90:123-151).
+// grid x_i = x0 + (i - 3 + o) dx, o = 1/2 on a periodic axis, 0 otherwise (grid.f90:123-151).
 static int upload_forcing(pcgb_box* b) {
   const pcgb_params& p = b->p;
   const size_t n = 2 * (size_t)b->px + 2 * (size_t)b->my + 2 * (size_t)b->mz;
   std::vector<double> h(n, 0.0);
-  const double dx = p.Lxyz[0] / p.nx, dy = p.Lxyz[1] / p.ny, dz = p.Lxyz[2] / p.nz;
+  const double dx = axis_spacing(p, 0), dy = axis_spacing(p, 1), dz = axis_spacing(p, 2);
+  const double ox = axis_offset(p, 0), oy = axis_offset(p, 1), oz = axis_offset(p, 2);
   double* sx = h.data(); double* cx = sx + b->px; double* sy = cx + b->px; double* cy = sy + b->my;
   double* sz = cy + b->my; double* cz = sz + b->mz;
-  for (int i = 0; i < b->mx; ++i) { double x = p.xyz0[0] + ((double)(i - 3) + 0.5) * dx; sx[i] = std::sin(p.kf * x); cx[i] = std::cos(p.kf * x); }
-  for (int i = 0; i < b->my; ++i) { double y = p.xyz0[1] + ((double)(i - 3) + 0.5) * dy; sy[i] = std::sin(p.kf * y); cy[i] = std::cos(p.kf * y); }
-  for (int i = 0; i < b->mz; ++i) { double z = p.xyz0[2] + ((double)(i - 3) + 0.5) * dz; sz[i] = std::sin(p.kf * z); cz[i] = std::cos(p.kf * z); }
+  for (int i = 0; i < b->mx; ++i) { double x = p.xyz0[0] + ((double)(i - 3) + ox) * dx; sx[i] = std::sin(p.kf * x); cx[i] = std::cos(p.kf * x); }
+  for (int i = 0; i < b->my; ++i) { double y = p.xyz0[1] + ((double)(i - 3) + oy) * dy; sy[i] = std::sin(p.kf * y); cy[i] = std::cos(p.kf * y); }
+  for (int i = 0; i < b->mz; ++i) { double z = p.xyz0[2] + ((double)(i - 3) + oz) * dz; sz[i] = std::sin(p.kf * z); cz[i] = std::cos(p.kf * z); }
   if (b->dfl) {   // double-float pairs: hi = nearest float, lo = nearest float to the rest
     std::vector<float> hf(2 * n);
     for (size_t i = 0; i < n; ++i) {
@@ -324,6 +345,20 @@ static int validate(const pcgb_params* p) {
     return set_err(PCGB_E_ARG, "lmagnetic_forcing applies to random helical forcing (lforcing_hel)");
   if ((p->lupw_uu != 0 && p->lupw_uu != 1) || (p->lupw_lnrho != 0 && p->lupw_lnrho != 1))
     return set_err(PCGB_E_ARG, "lupw_uu and lupw_lnrho must be 0 or 1");
+  const int nf = params_nf(*p);
+  for (int d = 0; d < 3; ++d) {
+    int nper = 0;
+    for (int k = 0; k < nf; ++k)
+      for (int side = 0; side < 2; ++side) {
+        const int c = p->bc[d][k][side];
+        if (c < PCGB_BC_PER || c > PCGB_BC_ASYM2)
+          return set_err(PCGB_E_ARG, "boundary condition code %d (direction %d, field %d) is not one of p, s, a, a2",
+                         c, d, k);
+        nper += (c == PCGB_BC_PER);
+      }
+    if (nper != 0 && nper != 2 * nf)
+      return set_err(PCGB_E_ARG, "direction %d mixes periodic and non-periodic boundary conditions", d);
+  }
   return 0;
 }
 
@@ -383,6 +418,7 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   d.f[0] = b->f[0]; d.f[1] = b->f[1]; d.df = b->df; d.forc = b->forc; d.state = b->dstate;
   d.nx = b->nx; d.ny = b->ny; d.nz = b->nz; d.px = b->px; d.my = b->my; d.mz = b->mz; d.xoff = b->xoff;
   d.nf = b->nf; d.ps = b->ps; d.fs = b->fs;
+  b->nonper = !(axis_periodic(*p, 0) && axis_periodic(*p, 1) && axis_periodic(*p, 2));
   fill_physics(b);
   if (upload_forcing(b) || set_tiling(b, p->tile, p->zdepth)) { box_free(b); return nullptr; }
   return b;
@@ -455,6 +491,10 @@ static bool box_needs_red(const pcgb_box* b, int mode) {
 }
 
 static int box_launch(pcgb_box* b, int mode) {
+  if (b->nonper) {   // ghosts of the non-periodic directions before every pass that reads f
+    const int rc = box_boundconds(b);
+    if (rc) return rc;
+  }
   if (mode == MODE_CFL && b->cfl_partial) {   // FP32 pairs: the light CFL pass
     CK(launch_cfl_pair(b->ddev, b->nf, b->nx, b->ny, b->nz, b->cfl_partial, b->cfl_done, g.stream));
     ++g.launches;
@@ -582,8 +622,9 @@ extern "C" int pcgb_box_init_field(pcgb_box* b, int field, int kind, double ampl
   const pcgb_params& p = b->p;
   const int comp = (field < 3) ? field : 0;   // ABC component of uu
   CK(launch_init_field(elem_code(b), base, kind, kind == 2 ? comp : 0, ampl, a, bb, c, k, seed, b->nx, b->ny, b->nz, b->px,
-                       b->my, b->xoff, p.xyz0[0], p.xyz0[1], p.xyz0[2], p.Lxyz[0] / p.nx, p.Lxyz[1] / p.ny,
-                       p.Lxyz[2] / p.nz, b->pairs ? 2 : 1, g.stream));
+                       b->my, b->xoff, p.xyz0[0], p.xyz0[1], p.xyz0[2], axis_spacing(p, 0), axis_spacing(p, 1),
+                       axis_spacing(p, 2), axis_offset(p, 0), axis_offset(p, 1), axis_offset(p, 2),
+                       b->pairs ? 2 : 1, g.stream));
   ++g.launches;
   return box_reset(b, 0.0);
 }
@@ -596,9 +637,14 @@ static int box_store_host(pcgb_box* b, void* fh, int hb) {
   const int in = cur_in(b);
   // the FP32 carry lives in df between steps (substep counter at a step boundary)
   const void* carry = (b->hdev.comp && (b->nsub % 3) == 0) ? b->df : nullptr;
+  if (b->nonper) {   // update_ghosts before the snapshot (snapshot.f90:363)
+    const int rc = box_boundconds(b);
+    if (rc) return rc;
+  }
+  const int permask = (axis_periodic(b->p, 0) ? 1 : 0) | (axis_periodic(b->p, 1) ? 2 : 0) | (axis_periodic(b->p, 2) ? 4 : 0);
   if (void* dh = const_cast<void*>(host_alias(fh))) {
     CK(launch_store_rows(elem_code(b), hb, dh, b->f[in], carry, 0, rows, b->nx, b->ny, b->nz, b->px,
-                         b->my, b->mz, b->xoff, b->nf, b->pairs, g.stream));
+                         b->my, b->mz, b->xoff, b->nf, b->pairs, permask, g.stream));
     ++g.launches;
     CK(cudaStreamSynchronize(g.stream));
     return box_check_state(b);
@@ -613,7 +659,7 @@ static int box_store_host(pcgb_box* b, void* fh, int hb) {
     const long long nr = std::min(chunk, rows - r0);
     CK(cudaStreamWaitEvent(g.stream, g.ev_free[k], 0));
     CK(launch_store_rows(elem_code(b), hb, g.stage[k], b->f[in], carry, r0, nr, b->nx, b->ny, b->nz, b->px, b->my, b->mz,
-                         b->xoff, b->nf, b->pairs, g.stream));
+                         b->xoff, b->nf, b->pairs, permask, g.stream));
     ++g.launches;
     CK(cudaEventRecord(g.ev_copied[k], g.stream));
     CK(cudaStreamWaitEvent(g.xfer, g.ev_copied[k], 0));
@@ -628,13 +674,6 @@ static int box_store_host(pcgb_box* b, void* fh, int hb) {
 
 extern "C" int pcgb_box_store(pcgb_box* b, double* fh) { return box_store_host(b, fh, 8); }
 extern "C" int pcgb_box_store_f32(pcgb_box* b, float* fh) { return box_store_host(b, fh, 4); }
-
-// Layout code of the helical forcing kernels.
-static int hel_layout(const pcgb_box* b) {
-  if (b->tb == 4) return b->pairs ? HEL_F32_PAIR : HEL_F32;
-  if (b->dfl) return b->pairs ? HEL_DD_PAIR : HEL_DD;
-  return HEL_F64;
-}
 
 // Random helical forcing of the step that starts now: draw its record into the
 // device ring (forcing.f90 fconst_coefs_hel), applied when the step ends.  With
@@ -659,7 +698,8 @@ static int helical_end_step(pcgb_box* b) {
   hg.nx = b->nx; hg.ny = b->ny; hg.nz = b->nz; hg.px = b->px; hg.my = b->my; hg.xoff = b->xoff;
   hg.ps = b->ps; hg.fs = b->fs;
   hg.x0 = p.xyz0[0]; hg.y0 = p.xyz0[1]; hg.z0 = p.xyz0[2];
-  hg.dx = p.Lxyz[0] / p.nx; hg.dy = p.Lxyz[1] / p.ny; hg.dz = p.Lxyz[2] / p.nz;
+  hg.dx = axis_spacing(p, 0); hg.dy = axis_spacing(p, 1); hg.dz = axis_spacing(p, 2);
+  hg.ox = axis_offset(p, 0); hg.oy = axis_offset(p, 1); hg.oz = axis_offset(p, 2);
   hg.k1 = p.kf;
   hg.iax = b->nf - 3;
   hg.magnetic = p.lmagnetic_forcing ? 1 : 0;
@@ -783,8 +823,9 @@ extern "C" pcgb_batch* pcgb_batch_create(pcgb_box** boxes, int n, int persistent
       return nullptr;
     }
     if (b->nsub % 3 != 0) { set_err(PCGB_E_STATE, "box in the middle of a step"); delete B; return nullptr; }
-    if (b->p.lforcing_hel) {
-      set_err(PCGB_E_UNSUPPORTED, "random helical forcing steps through the box API, not in a batch");
+    if (b->p.lforcing_hel || b->nonper) {
+      set_err(PCGB_E_UNSUPPORTED, "random helical forcing and non-periodic boundaries step through the box API, "
+                                  "not in a batch");
       delete B;
       return nullptr;
     }
@@ -1090,6 +1131,7 @@ static int box_reload(pcgb_box* b, const pcgb_params& p) {
     return set_err(PCGB_E_ARG, "reloadConfig cannot change grid, field count or precision");
   const int upw_was = b->hdev.lupw;
   b->p = p;
+  b->nonper = !(axis_periodic(p, 0) && axis_periodic(p, 1) && axis_periodic(p, 2));
   fill_physics(b);
   int rc = upload_forcing(b);
   if (rc) return rc;

@@ -20,6 +20,7 @@
 #include <thread>
 #include <vector>
 
+#include "boundcond.h"
 #include "../../include/pcgb300.h"
 #include "pcgb_box.h"
 
@@ -212,6 +213,8 @@ extern "C" long long pcgb_server_submit(pcgb_server* s, const pcgb_params* p, in
                                         double noise_ampl, double abc_ampl, double* f_out) {
   if (!s || !p || nsteps < 1) return -1;
   if (p->lforcing_hel) return -1;   // the step-end helical forcing runs through the box API only
+  for (int d = 0; d < 3; ++d)
+    if (!pcgb::axis_periodic(*p, d)) return -1;   // so do the ghost passes of non-periodic boundaries
   Req* r = new Req();
   r->p = *p;
   // (16,8) tiles suit small boxes: packed pairs for FP32 and double-float, field-major for FP64

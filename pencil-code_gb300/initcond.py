@@ -21,12 +21,9 @@ def field_index(p: Params, name: str) -> int:
 
 
 def grid(p: Params):
-    """Cell-centred periodic grid with ghosts, grid.f90:123-151."""
-    out = []
-    for i, n in enumerate((p.nx, p.ny, p.nz)):
-        d = p.Lxyz[i] / n
-        out.append(p.xyz0[i] + (np.arange(n + 6) - 3 + 0.5) * d)
-    return out
+    """The grid with ghosts, grid.f90:123-151: cell centres on a periodic axis,
+    points on both boundaries otherwise."""
+    return [p.axis(i) for i in range(3)]
 
 
 def zeros(p: Params) -> np.ndarray:

@@ -18,6 +18,8 @@ NSLOT = 10
 (S_DT1MAX, S_U2SUM, S_U2MAX, S_B2SUM, S_B2MAX, S_EKINSUM, S_RHOSUM, S_DIVB2SUM, S_J2SUM,
  S_ABSUM) = range(NSLOT)
 DT_FIXED, DT_LAGGED, DT_CURRENT = 0, 1, 2
+# boundary condition codes of pcgb_params.bc (boundcond.f90 bcx/bcy/bcz)
+BC_CODES = {"p": 0, "s": 1, "a": 2, "a2": 3}
 
 
 class Params(C.Structure):
@@ -39,15 +41,49 @@ class Params(C.Structure):
         ("tile", C.c_int), ("zdepth", C.c_int), ("dfloat", C.c_int),
         ("lforcing_hel", C.c_int), ("seed_ff", C.c_int), ("force_hel", C.c_double),
         ("lupw_uu", C.c_int), ("lupw_lnrho", C.c_int), ("lmagnetic_forcing", C.c_int), ("pad_", C.c_int),
+        ("bc", ((C.c_int * 2) * 8) * 3),
     ]
 
     def update(self, **kw) -> "Params":
+        """Set fields by name; bcx/bcy/bcz take one entry per field in f-array order,
+        each a code name ('p', 's', 'a', 'a2'), 'lower:upper', or a (lower, upper) pair."""
         for k, v in kw.items():
             if k in ("xyz0", "Lxyz", "b_ext"):
                 getattr(self, k)[:] = list(v)
+            elif k in ("bcx", "bcy", "bcz"):
+                self.set_bc("xyz".index(k[-1]), v)
             else:
                 setattr(self, k, v)
         return self
+
+    def set_bc(self, direction: int, entries) -> "Params":
+        for f in range(8):
+            self.bc[direction][f][0] = self.bc[direction][f][1] = 0
+        for f, e in enumerate(entries):
+            if isinstance(e, str):
+                lo, _, hi = e.strip().partition(":")
+                pair = (BC_CODES[lo.strip()], BC_CODES[(hi or lo).strip()])
+            elif isinstance(e, int):
+                pair = (e, e)
+            else:
+                pair = (int(e[0]), int(e[1]))
+            self.bc[direction][f][0], self.bc[direction][f][1] = pair
+        return self
+
+    def periodic(self, direction: int) -> bool:
+        nf = 8 if self.lentropy else 7
+        return all(self.bc[direction][f][s] == 0 for f in range(nf) for s in (0, 1))
+
+    def spacing(self, direction: int) -> float:
+        """grid.f90:123-151: L/n on a periodic axis, L/(n-1) otherwise."""
+        n = (self.nx, self.ny, self.nz)[direction]
+        return self.Lxyz[direction] / (n if self.periodic(direction) else n - 1)
+
+    def axis(self, direction: int) -> np.ndarray:
+        """Grid points of one axis with ghosts: x0 + (i - 3 + o) dx, o = 1/2 periodic, 0 otherwise."""
+        n = (self.nx, self.ny, self.nz)[direction]
+        o = 0.5 if self.periodic(direction) else 0.0
+        return self.xyz0[direction] + (np.arange(n + 6) - 3 + o) * self.spacing(direction)
 
     def as_dict(self) -> dict:
         out = {}

@@ -3,9 +3,10 @@
 Fortran namelist groups (`&name key=value, ... /`) as read by
 src/param_io.f90:82-250, :461-570, restricted to the keys of this hot path:
 
-  &init_pars            xyz0, Lxyz, lperi (all periodic here)
+  &init_pars            xyz0, Lxyz, lperi, bcx, bcy, bcz ('p', 's', 'a', 'a2', 'lower:upper')
   &eos_init_pars        gamma, cs0, rho0, cp
-  &run_pars             dt, nt, cdt, cdtv, itorder (3 only), it1, lbidiagonal_derij (T only)
+  &run_pars             dt, nt, cdt, cdtv, itorder (3 only), it1, lbidiagonal_derij (T only),
+                        bcx, bcy, bcz (override start.in's)
   &viscosity_run_pars   nu, ivisc ('nu-const' only)
   &magnetic_run_pars    eta, b_ext (B_ext), iresistivity ('eta-const' only)
   &entropy_run_pars     chi, iheatcond ('chi-const' only), lviscosity_heat
@@ -22,7 +23,7 @@ from __future__ import annotations
 
 import re
 
-from .lib import Params, default_params
+from .lib import BC_CODES, Params, default_params
 
 # one lexical item of a namelist body: a group start, a quoted string, the
 # group terminator '/', '=', ',' or a bare word (name, index, number, logical)
@@ -108,6 +109,32 @@ def _first(v):
     return v[0] if isinstance(v, list) else v
 
 
+def _listed(v) -> list:
+    return v if isinstance(v, list) else [v]
+
+
+def _boundary_conditions(p, init: dict, run: dict) -> None:
+    """lperi and bcx/bcy/bcz (cdata.f90 defaults: periodic, 'p'); run.in's bc lists
+    override start.in's.  Codes of this path: 'p', 's', 'a', 'a2', as 'lower:upper'
+    or one code for both sides; fields beyond the list keep 'p'."""
+    nf = 8 if p.lentropy else 7
+    lperi = [bool(v) for v in _listed(init.get("lperi", [True, True, True]))]
+    for d, key in enumerate(("bcx", "bcy", "bcz")):
+        per = lperi[d] if d < len(lperi) and lperi[d] is not None else True
+        vals = run.get(key, init.get(key))
+        entries = [str(v).strip().lower() for v in _listed(vals)][:nf] if vals is not None else []
+        entries += ["p"] * (nf - len(entries))
+        for e in entries:
+            for side in e.split(":"):
+                if side.strip() not in BC_CODES:
+                    raise ValueError(f"{key}={e!r}: only the boundary conditions p, s, a, a2 are implemented")
+        if per and any(e != "p" for e in entries):
+            raise ValueError(f"{key}={entries}: non-periodic conditions on a periodic direction (lperi=T)")
+        if not per and any("p" in e.split(":") for e in entries):
+            raise ValueError(f"{key}={entries}: lperi=F needs a non-periodic condition for every field")
+        p.set_bc(d, entries)
+
+
 def params_from_namelists(start_text: str, run_text: str, n=(32, 32, 32), lentropy: int = 0,
                           precision: int = 8) -> tuple[Params, dict, dict]:
     """Parameter block of a run; returns (params, initial-condition keys, keys not applied)."""
@@ -132,6 +159,7 @@ def params_from_namelists(start_text: str, run_text: str, n=(32, 32, 32), lentro
     init = sg.get("init_pars", {})
     if "xyz0" in init: p.xyz0[:] = [float(v) for v in init["xyz0"]]
     if "lxyz" in init: p.Lxyz[:] = [float(v) for v in init["lxyz"]]
+    _boundary_conditions(p, init, g.get("run_pars", {}))
     rp = g.get("run_pars", {})
     if "dt" in rp: p.dt = float(rp["dt"])
     if "cdt" in rp: p.cdt = float(rp["cdt"])
@@ -177,7 +205,7 @@ def params_from_namelists(start_text: str, run_text: str, n=(32, 32, 32), lentro
         if key in fr and _first(fr[key]) != default:
             raise ValueError(f"{key}={_first(fr[key])!r}: only the default {default!r} is implemented")
     known = {"run_pars": {"dt", "nt", "cdt", "cdtv", "itorder", "it1", "lbidiagonal_derij", "cvsid", "isave",
-                          "dsnap", "dvid", "dspec", "ou_spec", "ab_spec", "lpencil_check"},
+                          "dsnap", "dvid", "dspec", "ou_spec", "ab_spec", "lpencil_check", "bcx", "bcy", "bcz"},
              "viscosity_run_pars": {"nu", "ivisc"}, "magnetic_run_pars": {"eta", "b_ext", "iresistivity"},
              "entropy_run_pars": {"chi", "iheatcond", "lviscosity_heat"},
              "hydro_run_pars": {"lforcing_cont_uu", "ampl_fcont_uu", "lupw_uu"},

@@ -108,12 +108,10 @@ def read_dim(path: str) -> tuple[int, int, int, int]:
 
 
 def write_box_snapshot(path: str, p, f: np.ndarray, t: float) -> None:
-    """Snapshot of a box with the grid of grid.f90:123-151 (x_i = x0 + (i-3+1/2) dx)."""
-    dx, dy, dz = p.Lxyz[0] / p.nx, p.Lxyz[1] / p.ny, p.Lxyz[2] / p.nz
-    x = p.xyz0[0] + (np.arange(p.nx + 6) - 3 + 0.5) * dx
-    y = p.xyz0[1] + (np.arange(p.ny + 6) - 3 + 0.5) * dy
-    z = p.xyz0[2] + (np.arange(p.nz + 6) - 3 + 0.5) * dz
-    write_var(path, f, t, x, y, z, dx, dy, dz, precision=8)
+    """Snapshot of a box with the grid of grid.f90:123-151 (x_i = x0 + (i-3+1/2) dx on a
+    periodic axis, x0 + (i-3) dx with dx = L/(n-1) otherwise)."""
+    x, y, z = (p.axis(i) for i in range(3))
+    write_var(path, f, t, x, y, z, p.spacing(0), p.spacing(1), p.spacing(2), precision=8)
 
 
 def file_size(path: str) -> int:

@@ -42,7 +42,8 @@ def oracle_params(orc, p):
         lforcing_cont=p.lforcing_cont, ampl_ff=p.ampl_ff, kf=p.kf, relhel=p.relhel,
         abc_a=p.abc_a, abc_b=p.abc_b, abc_c=p.abc_c, ampl_fcont_uu=p.ampl_fcont_uu,
         b_ext=tuple(p.b_ext), lohmic_heat=p.lohmic_heat, lviscosity_heat=p.lviscosity_heat,
-        cdt=p.cdt, cdtv=p.cdtv, lupw_uu=p.lupw_uu, lupw_lnrho=p.lupw_lnrho)
+        cdt=p.cdt, cdtv=p.cdtv, lupw_uu=p.lupw_uu, lupw_lnrho=p.lupw_lnrho,
+        bc=[[[p.bc[a][f][0], p.bc[a][f][1]] for f in range(8)] for a in range(3)])
 
 
 def rel_err(a, b, log_fields=()):
