@@ -52,6 +52,10 @@ class Params(C.Structure):
                 getattr(self, k)[:] = list(v)
             elif k in ("bcx", "bcy", "bcz"):
                 self.set_bc("xyz".index(k[-1]), v)
+            elif k == "bc":   # the whole [3][8][2] table
+                for d in range(3):
+                    for f in range(8):
+                        self.bc[d][f][0], self.bc[d][f][1] = int(v[d][f][0]), int(v[d][f][1])
             else:
                 setattr(self, k, v)
         return self
@@ -86,11 +90,9 @@ class Params(C.Structure):
         return self.xyz0[direction] + (np.arange(n + 6) - 3 + o) * self.spacing(direction)
 
     def as_dict(self) -> dict:
-        out = {}
-        for name, _ in self._fields_:
-            v = getattr(self, name)
-            out[name] = list(v) if hasattr(v, "__len__") else v
-        return out
+        def plain(v):
+            return [plain(e) for e in v] if hasattr(v, "__len__") else v
+        return {name: plain(getattr(self, name)) for name, _ in self._fields_}
 
 
 _lib = None
