@@ -5,7 +5,8 @@ the start of that step, as the reference prints it) and var.dat snapshots every
 dsnap in time (data/proc0/VARn, then data/proc0/var.dat at the end), with the
 reference's dim.dat.
 
-Initial conditions of this path: zero fields, &magnetic_init_pars
+Boundary conditions and the grid follow lperi / bcx / bcy / bcz (periodic, or 's', 'a',
+'a2' per field and side).  Initial conditions of this path: zero fields, &magnetic_init_pars
 initaa='gaussian-noise' with amplaa (an N(0, amplaa^2) field from a seeded
 PCG64 stream; the reference's realisation comes from its own generator), and
 &hydro_init_pars inituu='ABC' with ampluu.  Anything else is refused.
@@ -72,13 +73,16 @@ def run(start_text: str, run_text: str, n, outdir: str, kdat=None, precision: in
     os.makedirs(proc, exist_ok=True)
     write_dim(os.path.join(data, "dim.dat"), p)
     f = initial_state(p, ic, seed)
-    write_box_snapshot(os.path.join(proc, "VAR0"), p, f, 0.0)
     box = Box(p)
     if p.lforcing_hel:
         if kdat is None:
             raise ValueError("iforce='helical' needs the wavevector list (k.dat)")
         box.set_kvectors(*kdat)
     box.load(f)
+    # VAR0 after update_ghosts (snapshot.f90:363): the device store fills the ghosts of
+    # non-periodic directions from their boundary conditions
+    write_box_snapshot(os.path.join(proc, "VAR0"), p, box.store() if not all(p.periodic(d) for d in range(3)) else f,
+                       0.0)
     rows, files = [], [os.path.join(proc, "VAR0")]
     ncells = p.nx * p.ny * p.nz
     tsnap, isnap = (dsnap if dsnap > 0 else math.inf), 0

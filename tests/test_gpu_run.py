@@ -66,3 +66,30 @@ def test_run_driver_helical_snapshots(tmp_path, pc):
           for i in range(1, nsnap + 1)]
     assert all(abs(t - 0.04 * round(t / 0.04)) < 1e-12 for t in ts) and ts == sorted(ts)
     assert all(t >= 0.1 * (i + 1) - 1e-9 and t < 0.1 * (i + 1) + 0.04 + 1e-9 for i, t in enumerate(ts))
+
+
+def test_run_driver_timing_namelists_with_boundaries(tmp_path, pc):
+    """The timing run's namelists (upwinding, helical forcing of aa) with z made
+    non-periodic ('s' for uu_x, uu_y, lnrho, A_x, A_y; 'a' for uu_z, A_z), on 24^3
+    with a small forcing shell: VAR0 and var.dat carry the boundary ghosts, the grid
+    record is the non-periodic one, and the final state is the box's own."""
+    run = importlib.import_module("pencil-code_gb300.run")
+    vd = importlib.import_module("pencil-code_gb300.vardat")
+    nl = importlib.import_module("pencil-code_gb300.namelist")
+    d = _json("timings_n4096_ref.json")
+    start = d["namelists"]["start.in"].replace(
+        "&init_pars", "&init_pars\n  lperi=T,T,F, bcz='s','s','a','s','s','s','a'", 1)
+    kdat = nl.kvector_shell(8, 12)
+    res = run.run(start, d["namelists"]["run.in"], (24, 24, 24), str(tmp_path), kdat=kdat, precision=4, nt=6)
+    p = res["params"]
+    assert p.lupw_uu == 1 and p.lmagnetic_forcing == 1 and not p.periodic(2)
+    var = vd.read_var(os.path.join(tmp_path, "data", "proc0", "var.dat"), 30, 30, 30, 7)
+    z = var["z"]
+    assert abs(z[3] + np.pi) < 1e-12 and abs(z[26] - np.pi) < 1e-12   # points on both boundaries
+    f = var["f"]
+    # 's' mirrors, 'a' mirrors with a sign change about a zero boundary value
+    assert np.array_equal(f[:, :, 2, 0], f[:, :, 4, 0]) and np.array_equal(f[:, :, 27, 3], f[:, :, 25, 3])
+    assert np.all(f[:, :, 3, 6] == 0.0) and np.array_equal(f[:, :, 1, 6], -f[:, :, 5, 6])
+    assert np.max(np.abs(f[3:-3, 3:-3, 3:-3, 4:7])) > 0.0   # aa forced
+    v0 = vd.read_var(os.path.join(tmp_path, "data", "proc0", "VAR0"), 30, 30, 30, 7)
+    assert np.all(np.isfinite(v0["f"])) and v0["t"] == 0.0
