@@ -87,9 +87,13 @@ def test_run_driver_timing_namelists_with_boundaries(tmp_path, pc):
     z = var["z"]
     assert abs(z[3] + np.pi) < 1e-12 and abs(z[26] - np.pi) < 1e-12   # points on both boundaries
     f = var["f"]
-    # 's' mirrors, 'a' mirrors with a sign change about a zero boundary value
-    assert np.array_equal(f[:, :, 2, 0], f[:, :, 4, 0]) and np.array_equal(f[:, :, 27, 3], f[:, :, 25, 3])
-    assert np.all(f[:, :, 3, 6] == 0.0) and np.array_equal(f[:, :, 1, 6], -f[:, :, 5, 6])
+    # 's' mirrors, 'a' mirrors with a sign change about a zero boundary value; in the FP32
+    # compensated state the interior is f + carry and a non-periodic ghost the condition
+    # applied to f, so they agree to FP32 rounding
+    def close(a, b):
+        return np.max(np.abs(a - b)) <= 2e-7 * max(np.max(np.abs(b)), 1e-30)
+    assert close(f[:, :, 2, 0], f[:, :, 4, 0]) and close(f[:, :, 27, 3], f[:, :, 25, 3])
+    assert np.all(f[:, :, 3, 6] == 0.0) and close(f[:, :, 1, 6], -f[:, :, 5, 6])
     assert np.max(np.abs(f[3:-3, 3:-3, 3:-3, 4:7])) > 0.0   # aa forced
     v0 = vd.read_var(os.path.join(tmp_path, "data", "proc0", "VAR0"), 30, 30, 30, 7)
     assert np.all(np.isfinite(v0["f"])) and v0["t"] == 0.0
