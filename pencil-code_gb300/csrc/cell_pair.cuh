@@ -11,6 +11,7 @@
 #pragma once
 
 #include "cell_physics.cuh"
+#include "helical_force.cuh"
 
 namespace pcgb {
 
@@ -20,7 +21,9 @@ __device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(
 __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 p_splat(float v) { return make_float2(v, v); }
 
-// UPW: compiled with the upwind corrections (lupw_uu, lupw_lnrho).
+// UPW: compiled with the upwind corrections (lupw_uu, lupw_lnrho) and with the
+// random helical force added in the last substep's update (the reference's
+// timing-run physics); the plain variants keep their registers.
 template <int NF, int TX, int TY, bool UPW = false>
 struct PairCell {
   using T = float;
@@ -128,6 +131,8 @@ struct PairCell {
     float fsz, fcz;   // sin/cos(kf z) of the current plane, prefetched one plane ahead
     float2 dfnext[4];
     int upw;          // UPW_* bits
+    const double* htab;   // helical forcing tables fused into the last substep, or null
+    int htarget;
 
     __device__ __forceinline__ void begin(const PcgbBoxDev& B, int inb, int x, int y, int z0, bool active,
                                           bool mode_cfl, const StepFlags<float>& fl) {
@@ -138,6 +143,8 @@ struct PairCell {
       ps = B.ps; fs = B.fs; px = B.px; xoff = B.xoff; nx = B.nx; ny = B.ny; nz = B.nz;
       forcing = B.lforcing != 0; iso = B.isothermal != 0; vheat = B.lviscosity_heat != 0; oheat = B.lohmic_heat != 0;
       upw = UPW ? B.lupw : 0;
+      htab = UPW ? B.hel_tab : nullptr;
+      htarget = B.hel_target;
       const float* sinx = reinterpret_cast<const float*>(B.forc);
       const float* cosx = sinx + B.px;
       const float* siny = cosx + B.px;
@@ -269,6 +276,17 @@ struct PairCell {
         }
       }
       if (!ENTROPY) { fnew[3].y = 0.f; dsto[3].y = 0.f; }
+      if constexpr (UPW) {
+        if (htab != nullptr && fl.s == 2) {   // forcing_hel after the step (addforce, forcing.f90:1307)
+          float fh[3];
+          helical_force_at(htab, nx, ny, x, y, z, fh);
+#pragma unroll
+          for (int p = 0; p < 3; ++p) {
+            if (htarget) fnew[p].y = __fadd_rn(fnew[p].y, fh[p]);
+            else fnew[p].x = __fadd_rn(fnew[p].x, fh[p]);
+          }
+        }
+      }
       if (fl.write_df) {
 #pragma unroll
         for (int p = 0; p < 4; ++p) dfp[p * fs + cidx] = dsto[p];

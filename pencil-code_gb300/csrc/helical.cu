@@ -17,6 +17,7 @@
 
 #include "dd.cuh"
 #include "helical.h"
+#include "helical_force.cuh"
 #include "mhd_common.cuh"
 
 namespace pcgb {
@@ -68,10 +69,12 @@ void helical_record(double cs0, double relhel, double force, const double* kxyz,
 }
 
 // tab: coef1[3], coef2[3], 2 spare, then fx, fy, fz as (re, im) pairs.
-__global__ void helical_tables_kernel(const HelRec* ring, const PcgbBoxState* S, double* tab, HelGeom g) {
-  const unsigned long long step = S->nsub / 3ull - 1ull;   // the step just completed
+// pre = 0: after the step (the step just completed, its dt_last); pre = 1: before
+// its last substep (the step in progress, its dt, for the fused update).
+__global__ void helical_tables_kernel(const HelRec* ring, const PcgbBoxState* S, double* tab, HelGeom g, int pre) {
+  const unsigned long long step = pre ? S->nsub / 3ull : S->nsub / 3ull - 1ull;
   const HelRec r = ring[step % (unsigned long long)kHelRing];
-  const double fact = __dmul_rn(r.fact0, sqrt(S->dt_last));
+  const double fact = __dmul_rn(r.fact0, sqrt(pre ? S->dt : S->dt_last));
   if (threadIdx.x < 3) {
     tab[threadIdx.x] = r.coef1[threadIdx.x];
     tab[3 + threadIdx.x] = r.coef2[threadIdx.x];
@@ -101,13 +104,6 @@ __global__ void helical_tables_kernel(const HelRec* ring, const PcgbBoxState* S,
   }
 }
 
-// arithmetic without contraction, in the precision of the state
-__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
 
 // The interior cell (x, y, z) and its periodic ghost images, as element offsets.
 struct CellImages {
@@ -215,13 +211,8 @@ __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
   if (i >= g.nx) return;
   const int k0 = blockIdx.z * kHelZ, k1 = min(k0 + kHelZ, g.nz);
   const int target = g.magnetic ? 1 : 0;
-  const double* fx = tab + 8;
-  const double* fy = fx + 2 * g.nx;
-  const double* fz = fy + 2 * g.ny;
-  const R xr = (R)fx[2 * i], xi = (R)fx[2 * i + 1];
-  const R yr = (R)fy[2 * j], yi = (R)fy[2 * j + 1];
-  const R pr = rsub(rmul(xr, yr), rmul(xi, yi)), pi = radd(rmul(xr, yi), rmul(xi, yr));   // fx fy
-  const R c1[3] = {(R)tab[0], (R)tab[1], (R)tab[2]}, c2[3] = {(R)tab[3], (R)tab[4], (R)tab[5]};
+  R pr, pi;
+  helical_fxy(tab, g.nx, i, j, pr, pi);   // fx fy
   E* sl[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) sl[c] = A::slice(f, g, target, c);
@@ -239,11 +230,11 @@ __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
     for (int u = 0; u < kHelB; ++u) {
       if (kb + u < k1) {
         const int k = kb + u;
-        const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
-        const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
+        R fh[3];
+        helical_fz(tab, g.nx, g.ny, k, pr, pi, fh);
         const CellImages ci(i, j, k, g);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) ci.store(sl[c], A::add(e[u][c], target, rsub(rmul(c1[c], qr), rmul(c2[c], qi))));
+        for (int c = 0; c < 3; ++c) ci.store(sl[c], A::add(e[u][c], target, fh[c]));
       }
     }
   }
@@ -252,7 +243,7 @@ __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
 cudaError_t launch_helical(int layout, void* f, const HelRec* ring, const PcgbBoxState* state, double* tab,
                            const HelGeom& g, cudaStream_t s) {
   if (g.ny > 65535 || g.nz > 65535) return cudaErrorInvalidValue;   // grid y/z limits
-  helical_tables_kernel<<<1, 256, 0, s>>>(ring, state, tab, g);
+  helical_tables_kernel<<<1, 256, 0, s>>>(ring, state, tab, g, 0);
   const dim3 grid((unsigned)((g.nx + 127) / 128), (unsigned)g.ny, (unsigned)((g.nz + kHelZ - 1) / kHelZ));
   switch (layout) {
     case HEL_F32: helical_apply_kernel<HEL_F32, float><<<grid, 128, 0, s>>>(f, tab, g); break;
@@ -261,6 +252,12 @@ cudaError_t launch_helical(int layout, void* f, const HelRec* ring, const PcgbBo
     case HEL_F32_PAIR: helical_apply_kernel<HEL_F32_PAIR, float><<<grid, 128, 0, s>>>(f, tab, g); break;
     default: helical_apply_kernel<HEL_DD_PAIR, double><<<grid, 128, 0, s>>>(f, tab, g); break;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_helical_tables_pre(const HelRec* ring, const PcgbBoxState* state, double* tab, const HelGeom& g,
+                                      cudaStream_t s) {
+  helical_tables_kernel<<<1, 256, 0, s>>>(ring, state, tab, g, 1);
   return cudaGetLastError();
 }
 

@@ -38,4 +38,9 @@ struct HelGeom {
 cudaError_t launch_helical(int layout, void* f, const HelRec* ring, const PcgbBoxState* state, double* tab,
                            const HelGeom& g, cudaStream_t s);
 
+// The tables of the step in progress (ring[(nsub/3) % kHelRing], its dt) before
+// its last substep, whose update adds the force itself (PcgbBoxDev::hel_tab).
+cudaError_t launch_helical_tables_pre(const HelRec* ring, const PcgbBoxState* state, double* tab, const HelGeom& g,
+                                      cudaStream_t s);
+
 }  // namespace pcgb

@@ -61,6 +61,11 @@ struct alignas(128) PcgbBoxDev {
   int diag_every;        // diagnostics at steps with step % diag_every == 0 (0: never)
   int isothermal;        // gamma == 1 without entropy
   int lupw;              // upwinding of u.grad u / u.grad lnrho (UPW_* bits)
+  // random helical forcing added in the last substep's update (FP32 pair layout):
+  // the step's tables (helical.cu layout: coef1[3] coef2[3] 2 spare, fx, fy, fz as
+  // (re, im) pairs), or null; the forced lane: 0 uu, 1 aa
+  const double* hel_tab;
+  int hel_target;
 };
 
 struct alignas(64) PcgbBoxState {

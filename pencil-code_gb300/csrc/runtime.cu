@@ -215,6 +215,10 @@ static void fill_physics(pcgb_box* b) {
   d.diag_every = p.diag_every;
   d.isothermal = (!p.lentropy && d.gamma_m1 == 0.0) ? 1 : 0;
   d.lupw = (p.lupw_uu ? UPW_UU : 0) | (p.lupw_lnrho ? UPW_LNRHO : 0);
+  // FP32 pairs with the upwinding kernel variant: the helical force is added in the
+  // last substep's update (otherwise by the apply kernel after the step)
+  d.hel_tab = (p.lforcing_hel && b->tb == 4 && b->pairs && d.lupw) ? b->dtab : nullptr;
+  d.hel_target = p.lmagnetic_forcing ? 1 : 0;
 }
 
 // ABC forcing tables sin/cos(kf*x) over the ghosted grid, forcing.f90:1100-1104,
@@ -691,8 +695,7 @@ static int helical_begin_step(pcgb_box* b) {
   return 0;
 }
 
-// addforce (forcing.f90:1307) after the step: uu (aa with magnetic forcing) of the new state += the force.
-static int helical_end_step(pcgb_box* b) {
+static HelGeom helical_geom(const pcgb_box* b) {
   const pcgb_params& p = b->p;
   HelGeom hg;
   hg.nx = b->nx; hg.ny = b->ny; hg.nz = b->nz; hg.px = b->px; hg.my = b->my; hg.xoff = b->xoff;
@@ -703,8 +706,20 @@ static int helical_end_step(pcgb_box* b) {
   hg.k1 = p.kf;
   hg.iax = b->nf - 3;
   hg.magnetic = p.lmagnetic_forcing ? 1 : 0;
-  CK(launch_helical(hel_layout(b), b->f[cur_in(b)], b->dring, b->dstate, b->dtab, hg, g.stream));
+  return hg;
+}
+
+// addforce (forcing.f90:1307) after the step: uu (aa with magnetic forcing) of the new state += the force.
+static int helical_end_step(pcgb_box* b) {
+  CK(launch_helical(hel_layout(b), b->f[cur_in(b)], b->dring, b->dstate, b->dtab, helical_geom(b), g.stream));
   g.launches += 2;
+  return 0;
+}
+
+// The same force added by the last substep's update itself (FP32 pairs): its tables first.
+static int helical_before_last_substep(pcgb_box* b) {
+  CK(launch_helical_tables_pre(b->dring, b->dstate, b->dtab, helical_geom(b), g.stream));
+  g.launches += 1;
   return 0;
 }
 
@@ -716,9 +731,11 @@ static int box_substep(pcgb_box* b) {
     if (b->hdev.dt_mode == PCGB_DT_CURRENT && (rc = box_launch(b, MODE_CFL))) return rc;
     if (b->p.lforcing_hel && (rc = helical_begin_step(b))) return rc;
   }
+  const bool fused = b->hdev.hel_tab != nullptr;
+  if (s == 2 && b->p.lforcing_hel && fused && (rc = helical_before_last_substep(b))) return rc;
   if ((rc = box_launch(b, MODE_SUBSTEP))) return rc;
   b->nsub++;
-  if (s == 2 && b->p.lforcing_hel && (rc = helical_end_step(b))) return rc;
+  if (s == 2 && b->p.lforcing_hel && !fused && (rc = helical_end_step(b))) return rc;
   return 0;
 }
 
