@@ -131,7 +131,7 @@ struct PairCell {
     float fsz, fcz;   // sin/cos(kf z) of the current plane, prefetched one plane ahead
     float2 dfnext[4];
     int upw;          // UPW_* bits
-    const double* htab;   // helical forcing tables fused into the last substep, or null
+    const float* htab;    // helical forcing tables (float copy) fused into the last substep, or null
     int htarget;
 
     __device__ __forceinline__ void begin(const PcgbBoxDev& B, int inb, int x, int y, int z0, bool active,

@@ -14,6 +14,7 @@
 // device (dt is the device's), and a second kernel applies them to every
 // interior cell and its periodic ghost images.
 #include <cmath>
+#include <type_traits>
 
 #include "dd.cuh"
 #include "helical.h"
@@ -82,25 +83,36 @@ __global__ void helical_tables_kernel(const HelRec* ring, const PcgbBoxState* S,
   double* fx = tab + 8;
   double* fy = fx + 2 * g.nx;
   double* fz = fy + 2 * g.ny;
+  // the same tables rounded to float, after the double ones (for FP32 states)
+  float* tabf = reinterpret_cast<float*>(tab + hel_tab_doubles(g.nx, g.ny, g.nz));
+  if (threadIdx.x < 3) {
+    tabf[threadIdx.x] = (float)r.coef1[threadIdx.x];
+    tabf[3 + threadIdx.x] = (float)r.coef2[threadIdx.x];
+  }
   for (int i = threadIdx.x; i < g.nx + g.ny + g.nz; i += blockDim.x) {
+    double re, im;
     if (i < g.nx) {
       const double x = __dadd_rn(g.x0, __dmul_rn((double)i + g.ox, g.dx));
       const double a = __dadd_rn(__dmul_rn(__dmul_rn(r.kk[0], g.k1), x), r.phase);
-      fx[2 * i] = __dmul_rn(cos(a), fact);
-      fx[2 * i + 1] = __dmul_rn(sin(a), fact);
+      re = __dmul_rn(cos(a), fact);
+      im = __dmul_rn(sin(a), fact);
     } else if (i < g.nx + g.ny) {
       const int j = i - g.nx;
       const double y = __dadd_rn(g.y0, __dmul_rn((double)j + g.oy, g.dy));
       const double a = __dmul_rn(__dmul_rn(r.kk[1], g.k1), y);
-      fy[2 * j] = cos(a);
-      fy[2 * j + 1] = sin(a);
+      re = cos(a);
+      im = sin(a);
     } else {
       const int k = i - g.nx - g.ny;
       const double z = __dadd_rn(g.z0, __dmul_rn((double)k + g.oz, g.dz));
       const double a = __dmul_rn(__dmul_rn(r.kk[2], g.k1), z);
-      fz[2 * k] = cos(a);
-      fz[2 * k + 1] = sin(a);
+      re = cos(a);
+      im = sin(a);
     }
+    fx[2 * i] = re;   // fx, fy, fz are consecutive
+    fx[2 * i + 1] = im;
+    tabf[8 + 2 * i] = (float)re;
+    tabf[8 + 2 * i + 1] = (float)im;
   }
 }
 
@@ -212,7 +224,11 @@ __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
   const int k0 = blockIdx.z * kHelZ, k1 = min(k0 + kHelZ, g.nz);
   const int target = g.magnetic ? 1 : 0;
   R pr, pi;
-  helical_fxy(tab, g.nx, i, j, pr, pi);   // fx fy
+  // FP32 layouts read the float copy of the tables (the same values (R)double gives)
+  using TT = typename std::conditional<sizeof(R) == 4, float, double>::type;
+  const TT* tt = (sizeof(R) == 4) ? reinterpret_cast<const TT*>(tab + hel_tab_doubles(g.nx, g.ny, g.nz))
+                                  : reinterpret_cast<const TT*>(tab);
+  helical_fxy(tt, g.nx, i, j, pr, pi);   // fx fy
   E* sl[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) sl[c] = A::slice(f, g, target, c);
@@ -231,7 +247,7 @@ __global__ void helical_apply_kernel(void* f, const double* tab, HelGeom g) {
       if (kb + u < k1) {
         const int k = kb + u;
         R fh[3];
-        helical_fz(tab, g.nx, g.ny, k, pr, pi, fh);
+        helical_fz(tt, g.nx, g.ny, k, pr, pi, fh);
         const CellImages ci(i, j, k, g);
 #pragma unroll
         for (int c = 0; c < 3; ++c) ci.store(sl[c], A::add(e[u][c], target, fh[c]));

@@ -15,6 +15,13 @@ struct HelRec {
 
 constexpr int kHelRing = 64;   // records kept on the device, indexed by step % kHelRing
 
+// Size of a step's tables: coef1[3], coef2[3], 2 spare, fx[nx], fy[ny], fz[nz] as
+// (re, im) doubles, followed by the same values rounded to float (for FP32 states).
+__host__ __device__ inline long long hel_tab_doubles(int nx, int ny, int nz) { return 8 + 2LL * (nx + ny + nz); }
+__host__ __device__ inline size_t hel_tab_bytes(int nx, int ny, int nz) {
+  return (size_t)hel_tab_doubles(nx, ny, nz) * (sizeof(double) + sizeof(float));
+}
+
 // Draw the record of the next step from the ran0 stream `state` (two draws for
 // phase and wavevector, one for the polarisation angle, as the reference draws them).
 void helical_record(double cs0, double relhel, double force, const double* kxyz, int nk, double kav, int* state,

@@ -15,11 +15,11 @@ __device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
 
-// fx(i) fy(j)
-template <typename R>
-__device__ __forceinline__ void helical_fxy(const double* tab, int nx, int i, int j, R& pr, R& pi) {
-  const double* fx = tab + 8;
-  const double* fy = fx + 2 * nx;
+// fx(i) fy(j); T: the table's element type (double, or its float copy)
+template <typename R, typename T>
+__device__ __forceinline__ void helical_fxy(const T* tab, int nx, int i, int j, R& pr, R& pi) {
+  const T* fx = tab + 8;
+  const T* fy = fx + 2 * nx;
   const R xr = (R)fx[2 * i], xi = (R)fx[2 * i + 1];
   const R yr = (R)fy[2 * j], yi = (R)fy[2 * j + 1];
   pr = rsub(rmul(xr, yr), rmul(xi, yi));
@@ -27,17 +27,17 @@ __device__ __forceinline__ void helical_fxy(const double* tab, int nx, int i, in
 }
 
 // the three force components at plane k from fx fy = (pr, pi)
-template <typename R>
-__device__ __forceinline__ void helical_fz(const double* tab, int nx, int ny, int k, R pr, R pi, R out[3]) {
-  const double* fz = tab + 8 + 2 * nx + 2 * ny;
+template <typename R, typename T>
+__device__ __forceinline__ void helical_fz(const T* tab, int nx, int ny, int k, R pr, R pi, R out[3]) {
+  const T* fz = tab + 8 + 2 * nx + 2 * ny;
   const R zr = (R)fz[2 * k], zi = (R)fz[2 * k + 1];
   const R qr = rsub(rmul(pr, zr), rmul(pi, zi)), qi = radd(rmul(pr, zi), rmul(pi, zr));   // (fx fy) fz
 #pragma unroll
   for (int c = 0; c < 3; ++c) out[c] = rsub(rmul((R)tab[c], qr), rmul((R)tab[3 + c], qi));
 }
 
-template <typename R>
-__device__ __forceinline__ void helical_force_at(const double* tab, int nx, int ny, int i, int j, int k, R out[3]) {
+template <typename R, typename T>
+__device__ __forceinline__ void helical_force_at(const T* tab, int nx, int ny, int i, int j, int k, R out[3]) {
   R pr, pi;
   helical_fxy(tab, nx, i, j, pr, pi);
   helical_fz(tab, nx, ny, k, pr, pi, out);

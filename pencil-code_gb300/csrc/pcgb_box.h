@@ -62,9 +62,9 @@ struct alignas(128) PcgbBoxDev {
   int isothermal;        // gamma == 1 without entropy
   int lupw;              // upwinding of u.grad u / u.grad lnrho (UPW_* bits)
   // random helical forcing added in the last substep's update (FP32 pair layout):
-  // the step's tables (helical.cu layout: coef1[3] coef2[3] 2 spare, fx, fy, fz as
-  // (re, im) pairs), or null; the forced lane: 0 uu, 1 aa
-  const double* hel_tab;
+  // the float copy of the step's tables (helical.h: coef1[3] coef2[3] 2 spare, fx,
+  // fy, fz as (re, im) pairs), or null; the forced lane: 0 uu, 1 aa
+  const float* hel_tab;
   int hel_target;
 };
 

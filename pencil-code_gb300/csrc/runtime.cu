@@ -217,7 +217,9 @@ static void fill_physics(pcgb_box* b) {
   d.lupw = (p.lupw_uu ? UPW_UU : 0) | (p.lupw_lnrho ? UPW_LNRHO : 0);
   // FP32 pairs with the upwinding kernel variant: the helical force is added in the
   // last substep's update (otherwise by the apply kernel after the step)
-  d.hel_tab = (p.lforcing_hel && b->tb == 4 && b->pairs && d.lupw) ? b->dtab : nullptr;
+  d.hel_tab = (p.lforcing_hel && b->tb == 4 && b->pairs && d.lupw)
+                  ? reinterpret_cast<const float*>(b->dtab + hel_tab_doubles(b->nx, b->ny, b->nz))
+                  : nullptr;
   d.hel_target = p.lmagnetic_forcing ? 1 : 0;
 }
 
@@ -401,7 +403,7 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   if (cudaMalloc(&b->dstate, sizeof(PcgbBoxState)) != cudaSuccess) return fail("state");
   if (cudaMalloc(&b->ddev, sizeof(PcgbBoxDev)) != cudaSuccess) return fail("descriptor");
   if (cudaMalloc(&b->dring, sizeof(HelRec) * kHelRing) != cudaSuccess ||
-      cudaMalloc(&b->dtab, sizeof(double) * (8 + 2 * ((size_t)b->nx + b->ny + b->nz))) != cudaSuccess)
+      cudaMalloc(&b->dtab, hel_tab_bytes(b->nx, b->ny, b->nz)) != cudaSuccess)
     return fail("helical forcing tables");
   if (b->tb == 4 && b->pairs) {
     if (cudaMalloc(&b->cfl_partial, sizeof(double) * cfl_pair_blocks(b->nx, b->ny, b->nz)) != cudaSuccess ||
