@@ -133,6 +133,8 @@ struct PairCell {
     int upw;          // UPW_* bits
     const float* htab;    // helical forcing tables (float copy) fused into the last substep, or null
     int htarget;
+    float hpr, hpi;       // fx fy of this column
+    float hc1[3], hc2[3]; // coef1, coef2 of the step
 
     __device__ __forceinline__ void begin(const PcgbBoxDev& B, int inb, int x, int y, int z0, bool active,
                                           bool mode_cfl, const StepFlags<float>& fl) {
@@ -145,6 +147,13 @@ struct PairCell {
       upw = UPW ? B.lupw : 0;
       htab = UPW ? B.hel_tab : nullptr;
       htarget = B.hel_target;
+      if constexpr (UPW) {
+        if (htab != nullptr && fl.s == 2 && active) {   // the step's tables are in place before the last substep
+          helical_fxy(htab, nx, x, y, hpr, hpi);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) { hc1[c] = htab[c]; hc2[c] = htab[3 + c]; }
+        }
+      }
       const float* sinx = reinterpret_cast<const float*>(B.forc);
       const float* cosx = sinx + B.px;
       const float* siny = cosx + B.px;
@@ -169,6 +178,14 @@ struct PairCell {
                                          const StepFlags<float>& fl, Acc& acc, float& dt1max) {
       const St st{pl, F};
       const long long cidx = (long long)(z + 3) * ps + (long long)(y + 3) * px + xoff + x;
+      float hzr = 0.f, hzi = 0.f;   // fz of this plane, loaded ahead of its use at the update
+      if constexpr (UPW) {
+        if (htab != nullptr && fl.s == 2) {
+          const float* fz = htab + 8 + 2 * nx + 2 * ny;
+          hzr = fz[2 * z];
+          hzi = fz[2 * z + 1];
+        }
+      }
       float2 dfo2[4];
 #pragma unroll
       for (int p = 0; p < 4; ++p) dfo2[p] = dfnext[p];
@@ -278,12 +295,13 @@ struct PairCell {
       if (!ENTROPY) { fnew[3].y = 0.f; dsto[3].y = 0.f; }
       if constexpr (UPW) {
         if (htab != nullptr && fl.s == 2) {   // forcing_hel after the step (addforce, forcing.f90:1307)
-          float fh[3];
-          helical_force_at(htab, nx, ny, x, y, z, fh);
+          // (fx fy) fz and Re[(coef1 + i coef2) fxyz], as helical_fz computes them
+          const float qr = rsub(rmul(hpr, hzr), rmul(hpi, hzi)), qi = radd(rmul(hpr, hzi), rmul(hpi, hzr));
 #pragma unroll
           for (int p = 0; p < 3; ++p) {
-            if (htarget) fnew[p].y = __fadd_rn(fnew[p].y, fh[p]);
-            else fnew[p].x = __fadd_rn(fnew[p].x, fh[p]);
+            const float fh = rsub(rmul(hc1[p], qr), rmul(hc2[p], qi));
+            if (htarget) fnew[p].y = __fadd_rn(fnew[p].y, fh);
+            else fnew[p].x = __fadd_rn(fnew[p].x, fh);
           }
         }
       }
