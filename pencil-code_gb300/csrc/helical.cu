@@ -12,7 +12,9 @@
 // The host draws each step's wavevector, phase and polarisation angle; a
 // one-block kernel builds the 1-D factor tables of the completed step on the
 // device (dt is the device's), and a second kernel applies them to every
-// interior cell and its periodic ghost images.
+// interior cell and its periodic ghost images.  For a box in the FP32 pair
+// layout running the upwinding kernel variant the tables are built before the
+// step's last substep and that substep's update adds the force (helical_force.cuh).
 #include <cmath>
 #include <type_traits>
 
