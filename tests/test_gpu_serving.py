@@ -69,3 +69,35 @@ def test_admission_budget_and_fifo(pc):
         srv.close()
         # requests that arrive while a round runs join at the next round boundary
         assert lo <= st["peak_active"] <= hi and st["peak_bytes"] <= budget
+
+
+def test_upwinding_requests_in_the_mix(pc):
+    """Requests with upwinded advection (their own kernel variant, so their own class in
+    the batched launch) served together with plain ones: each result equals the box alone.
+    Requests the batched launch cannot take (helical forcing, non-periodic boundaries)
+    are refused at submission."""
+    serve = importlib.import_module("pencil-code_gb300.serve")
+    ens = importlib.import_module("pencil-code_gb300.ensemble")
+    specs = [(32, 4, False, 21, 2e-3, 1.0, 6, 1), (32, 4, False, 22, 3e-3, 2.0, 6, 0), (24, 8, False, 23, 5e-3, 1.0, 5, 1),
+             (24, 8, True, 24, 4e-3, 2.0, 5, 1), (16, 9, False, 25, 6e-3, 1.0, 7, 1), (40, 4, True, 26, 2e-3, 1.0, 4, 1)]
+
+    def req(n, prec, ent, seed, nu, k, upw):
+        return _req(pc, n, prec, ent, seed, nu, k).update(lupw_uu=upw, lupw_lnrho=upw)
+
+    srv = serve.Server(budget_bytes=20e9, round_steps=2)
+    outs, ids = [], []
+    for n, prec, ent, seed, nu, k, steps, upw in specs:
+        p = req(n, prec, ent, seed, nu, k, upw)
+        f = np.zeros(pc.host_shape(p), order="F")
+        outs.append(f)
+        ids.append(srv.submit(p, steps, seed, noise=1e-5, f_out=f))
+    with pytest.raises(pc.PcgbError):
+        srv.submit(req(16, 4, False, 30, 2e-3, 1.0, 0).update(lforcing_hel=1, force_hel=0.05), 3, 30)
+    with pytest.raises(pc.PcgbError):
+        srv.submit(req(16, 4, False, 31, 2e-3, 1.0, 0).update(bcz=["s"] * 7), 3, 31)
+    assert srv.drain(600)
+    assert all(srv.poll(rid)[0] == 1 for rid in ids)
+    srv.close()
+    for (n, prec, ent, seed, nu, k, steps, upw), f in zip(specs, outs):
+        ref = _alone(pc, ens, req(n, prec, ent, seed, nu, k, upw), steps, seed)
+        assert np.array_equal(f, ref), (n, prec, ent, upw)
