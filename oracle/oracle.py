@@ -19,7 +19,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 NGHOST = 3
 
-D_U2SUM, D_U2MAX, D_B2SUM, D_B2MAX, D_EKINSUM, D_RHOSUM, D_DIVB2SUM, D_J2SUM, D_ABSUM, D_N = range(10)
+(D_U2SUM, D_U2MAX, D_B2SUM, D_B2MAX, D_EKINSUM, D_RHOSUM, D_DIVB2SUM, D_J2SUM, D_ABSUM, D_JBSUM, D_EPSKSUM,
+ D_N) = range(12)
 
 
 class OrcParams(C.Structure):
@@ -80,6 +81,7 @@ def lib():
         L.orc_ran0.argtypes = [C.POINTER(C.c_int)]
         L.orc_ran0.restype = C.c_double
         L.orc_gaunoise_vect.argtypes = [P, C.c_double, dp, C.c_int, C.c_int, C.POINTER(C.c_int)]
+        L.orc_gaunoise_volume.argtypes = [P, C.c_double, dp, C.c_int, C.c_int, C.POINTER(C.c_int)]
         L.orc_grid.argtypes = [P, dpc, dpc, dpc]
         L.orc_helical_coefs.argtypes = [P, C.c_double, dpc, dpc, dpc, C.c_int, C.c_double, C.POINTER(C.c_int),
                                         C.POINTER(HelRec)]
@@ -191,6 +193,14 @@ def gaunoise_vect(p: OrcParams, ampl: float, f: np.ndarray, i1: int, i2: int, st
     return s.value
 
 
+def gaunoise_volume(p: OrcParams, ampl: float, f: np.ndarray, i1: int, i2: int, state: int) -> int:
+    """gaunoise_vect's draws over whole (mx,my,mz) arrays in random_number_wrapper_3's
+    order (z fastest): the realisation of samples/MHD-ABCforcing/reference.out."""
+    s = C.c_int(state)
+    lib().orc_gaunoise_volume(C.byref(p), ampl, f, i1, i2, C.byref(s))
+    return s.value
+
+
 def diag_summary(p: OrcParams, dg: np.ndarray) -> dict:
     """Volume averages as the reference prints them (diagnostics.f90:274,
     hydro.f90:4709,4743, magnetic.f90:6879,6894)."""
@@ -199,4 +209,5 @@ def diag_summary(p: OrcParams, dg: np.ndarray) -> dict:
                 brms=np.sqrt(dg[D_B2SUM] / nw), bmax=np.sqrt(dg[D_B2MAX]),
                 ekin=dg[D_EKINSUM] / nw, rhom=dg[D_RHOSUM] / nw,
                 divbrms=np.sqrt(dg[D_DIVB2SUM] / nw), jrms=np.sqrt(dg[D_J2SUM] / nw),
-                abm=dg[D_ABSUM] / nw)
+                abm=dg[D_ABSUM] / nw, jbm=dg[D_JBSUM] / nw, epsK=dg[D_EPSKSUM] / nw,
+                epsM=p.eta * p.mu0 * dg[D_J2SUM] / nw)

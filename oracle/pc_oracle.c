@@ -120,6 +120,10 @@ static void bc_side(const orc_params* p, const ctx_t* c, double* f, int k, int d
   const int na = d == 0 ? c->my : c->mx, nb = d == 0 ? c->mz : (d == 1 ? c->mz : c->my);
   const size_t st = d == 0 ? 1 : d == 1 ? (size_t)c->mx : (size_t)c->mx * c->my;
   const int b1 = NG, b2 = NG + n - 1;   /* n1, n2 (0-based array indices) */
+  /* the lines normal to the boundary are independent: threads change nothing */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) if ((size_t)na * nb > 4096)
+#endif
   for (int ib = 0; ib < nb; ++ib)
     for (int ia = 0; ia < na; ++ia) {
       size_t base;   /* element at index 0 along d */
@@ -353,6 +357,7 @@ static double cell(const orc_params* p, const ctx_t* c, const double* f, double*
   }
   double del2a[3];   /* gij_etc, sub.f90:3085 */
   for (int i = 0; i < 3; ++i) del2a[i] = (d2A[0][0][i] + d2A[1][1][i]) + d2A[2][2][i];
+  const double bbb[3] = {bb[0], bb[1], bb[2]};   /* p%bbb: B before B_ext, magnetic.f90:4356 */
   for (int j = 0; j < 3; ++j) bb[j] = bb[j] + p->b_ext[j];   /* B_ext, magnetic.f90:4366-4370 */
   double jj[3];   /* jj = mu01*curl(bij), magnetic.f90:4735 */
   jj[0] = c->mu01 * (bij[2][1] - bij[1][2]);
@@ -439,7 +444,7 @@ static double cell(const orc_params* p, const ctx_t* c, const double* f, double*
   if (dg) {
     double rho = exp(lnrho);
     double divb = (bij[0][0] + bij[1][1]) + bij[2][2];
-    double ab = (aa[0] * bb[0] + aa[1] * bb[1]) + aa[2] * bb[2];
+    double ab = (aa[0] * bbb[0] + aa[1] * bbb[1]) + aa[2] * bbb[2];   /* p%ab = aa.bbb, magnetic.f90:4451 */
     dg[ORC_D_U2SUM] += u2;
     if (u2 > dg[ORC_D_U2MAX]) dg[ORC_D_U2MAX] = u2;
     dg[ORC_D_B2SUM] += b2;
@@ -449,6 +454,8 @@ static double cell(const orc_params* p, const ctx_t* c, const double* f, double*
     dg[ORC_D_DIVB2SUM] += divb * divb;
     dg[ORC_D_J2SUM] += j2;
     dg[ORC_D_ABSUM] += ab;
+    dg[ORC_D_JBSUM] += (jj[0] * bbb[0] + jj[1] * bbb[1]) + jj[2] * bbb[2];   /* p%jb = jj.bbb, magnetic.f90:4781 */
+    dg[ORC_D_EPSKSUM] += ((2.0 * p->nu) * sij2) * rho;                      /* visc_heat*rho, viscosity.f90:2908 */
   }
   return dt1;
 }
@@ -506,15 +513,24 @@ void orc_time_step(const orc_params* p, double* f, double* df, double* t, double
     double dt1 = 0.0;
     /* substep 1 with df = 0 (alpha = 0 makes alpha*df = 0 for finite df) */
     if (itsub == 0) {
-      size_t ntot = (size_t)mx * my * (p->nz + 2 * NG) * nf;
-      memset(df, 0, ntot * sizeof(double));
+      const size_t nfield = (size_t)mx * my * (p->nz + 2 * NG);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+      for (int k = 0; k < nf * (p->nz + 2 * NG); ++k)
+        memset(df + (size_t)k * (nfield / (p->nz + 2 * NG)), 0, nfield / (p->nz + 2 * NG) * sizeof(double));
     }
     orc_pde(p, f, df, alpha, ldt && itsub == 0, &dt1, itsub == 0 ? diag : NULL, nthreads);
     if (ldt && itsub == 0) *dt = 1.0 / dt1;          /* set_dt, sub.f90:4247 */
     ds = ds + 1.0;
     double dt_beta = *dt * beta_ts[itsub];
     double dtsub = ds * dt_beta;
-    for (int k = 0; k < nf; ++k)                      /* timestep.f90:160-161 */
+    /* timestep.f90:160-161; every element is independent, so the threads
+       change nothing in the result */
+#ifdef _OPENMP
+#pragma omp parallel for collapse(2) schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+    for (int k = 0; k < nf; ++k)
       for (int n = NG; n < NG + p->nz; ++n)
         for (int m = NG; m < NG + p->ny; ++m) {
           size_t o = (size_t)mx * ((size_t)m + (size_t)my * ((size_t)n + (size_t)(p->nz + 2 * NG) * k));
@@ -560,6 +576,36 @@ void orc_gaunoise_vect(const orc_params* p, double ampl, double* f, int i1, int 
           for (int l = 0; l < mx; ++l) f[o + l] = f[o + l] + ampl * (sqrt(-2.0 * log(r[l])) * cos((2.0 * pi) * q[l]));
         }
       }
+  free(r); free(q);
+}
+
+/* gaunoise_vect's draws and sin/cos pairing (initcond.f90:5026-5040) with
+   volume arrays filled by random_number_wrapper_3 (general.f90:733-739): the
+   loops run x outermost and z innermost, so consecutive draws step along z.
+   The reference.out of samples/MHD-ABCforcing (brms 1.684E-01, jbm 2.24E-03,
+   b1b32m 2.17E-04, epsM 8.11E-01, abm 9.67E-06 at it=0) is this realisation
+   of seed -10; the pencil-wise fill of orc_gaunoise_vect is not. */
+void orc_gaunoise_volume(const orc_params* p, double ampl, double* f, int i1, int i2, int* state) {
+  const size_t mx = (size_t)p->nx + 2 * NG, my = (size_t)p->ny + 2 * NG, mz = (size_t)p->nz + 2 * NG;
+  const size_t nv = mx * my * mz;
+  const double pi = 3.14159265358979323846264338327950;
+  if (ampl == 0.0) return;
+  double* r = malloc(sizeof(double) * nv);
+  double* q = malloc(sizeof(double) * nv);
+  for (int i = i1; i <= i2; ++i) {
+    double* fi = f + nv * (size_t)i;
+    if ((i - i1) % 2 == 0) {
+      for (size_t l = 0; l < mx; ++l)          /* random_number_wrapper_3(r) */
+        for (size_t m = 0; m < my; ++m)
+          for (size_t n = 0; n < mz; ++n) r[l + mx * (m + my * n)] = orc_ran0(state);
+      for (size_t l = 0; l < mx; ++l)          /* random_number_wrapper_3(p) */
+        for (size_t m = 0; m < my; ++m)
+          for (size_t n = 0; n < mz; ++n) q[l + mx * (m + my * n)] = orc_ran0(state);
+      for (size_t o = 0; o < nv; ++o) fi[o] = fi[o] + ampl * (sqrt(-2.0 * log(r[o])) * sin((2.0 * pi) * q[o]));
+    } else {
+      for (size_t o = 0; o < nv; ++o) fi[o] = fi[o] + ampl * (sqrt(-2.0 * log(r[o])) * cos((2.0 * pi) * q[o]));
+    }
+  }
   free(r); free(q);
 }
 

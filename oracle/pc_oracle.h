@@ -42,7 +42,7 @@ enum { ORC_BC_PER = 0, ORC_BC_SYM = 1, ORC_BC_ASYM = 2, ORC_BC_ASYM2 = 3 };
 /* Diagnostic slots (FP64), evaluated on f at the start of a step. */
 enum {
   ORC_D_U2SUM = 0, ORC_D_U2MAX, ORC_D_B2SUM, ORC_D_B2MAX, ORC_D_EKINSUM,
-  ORC_D_RHOSUM, ORC_D_DIVB2SUM, ORC_D_J2SUM, ORC_D_ABSUM, ORC_D_N
+  ORC_D_RHOSUM, ORC_D_DIVB2SUM, ORC_D_J2SUM, ORC_D_ABSUM, ORC_D_JBSUM, ORC_D_EPSKSUM, ORC_D_N
 };
 
 int  orc_nfields(const orc_params* p);
@@ -98,6 +98,11 @@ void orc_add_helical(const orc_params* p, double* f, const orc_helrec* rec, doub
    gaunoise_vect (src/initcond.f90:5005-5047). */
 double orc_ran0(int* state);
 void orc_gaunoise_vect(const orc_params* p, double ampl, double* f, int i1, int i2, int* state);
+/* The same Box-Muller pairing over whole volumes: per drawn component one
+   (mx,my,mz) array of radii and one of phases, each filled by
+   random_number_wrapper_3 (src/general.f90:733-739: z fastest, x slowest).
+   This is the realisation printed in samples/MHD-ABCforcing/reference.out. */
+void orc_gaunoise_volume(const orc_params* p, double ampl, double* f, int i1, int i2, int* state);
 
 #ifdef __cplusplus
 }

@@ -161,8 +161,10 @@ __device__ __forceinline__ void cell_rhs(const CellIn<T>& c, const Phys<T>& P, c
   if (want_diag) {
     const T b00 = c.a3xy - c.a2xz, b11 = c.a1yz - c.a3xy, b22 = c.a2xz - c.a1yz;
     const double divb = (double)((b00 + b11) + b22);
-    const double ab = ((double)c.aa[0] * (double)bb[0] + (double)c.aa[1] * (double)bb[1]) +
-                      (double)c.aa[2] * (double)bb[2];
+    // <A.B> uses the field before the imposed B_ext is added (p%bbb, magnetic.f90:4356,4451)
+    const T bbb0 = c.aij[2][1] - c.aij[1][2], bbb1 = c.aij[0][2] - c.aij[2][0], bbb2 = c.aij[1][0] - c.aij[0][1];
+    const double ab = ((double)c.aa[0] * (double)bbb0 + (double)c.aa[1] * (double)bbb1) +
+                      (double)c.aa[2] * (double)bbb2;
     acc_diag(acc, (double)u2, (double)b2, (double)c.lnrho, divb, (double)j2, ab);
   }
 }

@@ -1,16 +1,16 @@
 """Generate the golden vectors used by tests/test_oracle_golden.py.
 
-Run in a container where the reference tree is mounted (it is read here and
-nowhere else):
+Run where the pencil-code source tree is available (it is read here and
+nowhere else), giving its path as the argument or in PENCIL_REFERENCE:
 
-    python tests/golden/gen_golden.py /root/reference
+    python tests/golden/gen_golden.py <path of the pencil-code tree>
 
 1. stencils.npz -- first and second derivatives of seeded random periodic
    fields computed by the reference's own numpy module
    python/pencil/math/derivatives/der_6th_order_w_ghosts.py (xder_6th ...
    zder2_6th), loaded standalone (the package-level import needs h5py).
 2. mhd_abcforcing_ref.json -- the it / dt / urms / umax / brms columns of
-   samples/MHD-ABCforcing/reference.out, the reference's regression series
+   samples/MHD-ABCforcing/reference.out (and every column as printed text), the reference's regression series
    for isothermal MHD with continuous ABC forcing, with the run parameters of
    that sample's start.in / run.in, and the text of those two namelist files.
 3. var_sample_1d.dat / var_sample_1d.json -- the var.dat snapshot committed
@@ -90,14 +90,19 @@ def main(ref_root):
 
     # regression series of samples/MHD-ABCforcing (read as text)
     sample = os.path.join(ref_root, "samples", "MHD-ABCforcing")
-    rows = []
+    rows, printed = [], []
     with open(os.path.join(sample, "reference.out")) as fh:
         for line in fh:
-            if line.startswith("#") or not line.strip():
+            if line.startswith("#"):
+                cols = [c for c in line.strip("#\n").split("-") if c]
+                continue
+            if not line.strip():
                 continue
             v = line.split()
             rows.append({"it": int(v[0]), "t": float(v[1]), "dt": float(v[2]), "urms": float(v[3]),
                          "umax": float(v[4]), "brms": float(v[5])})
+            # every column as printed, so a test can take its tolerance from the printed digits
+            printed.append(dict(zip(cols, v)))
     params = {"n": 32, "gamma": 1.0, "nu": 0.1, "eta": 0.1, "ampl_ff": 1e-4, "k1_ff": 1.0,
               "iforcing_cont": "ABC", "b_ext": [0.0, 0.1, 0.0], "cdt": 0.4, "amplaa": 1e-2,
               "initaa": "gaussian-noise", "nt": 51, "it1": 10,
@@ -107,7 +112,7 @@ def main(ref_root):
         with open(os.path.join(sample, name)) as fh:
             namelists[name] = fh.read()
     with open(os.path.join(here, "mhd_abcforcing_ref.json"), "w") as fh:
-        json.dump({"params": params, "series": rows, "namelists": namelists}, fh, indent=1)
+        json.dump({"params": params, "series": rows, "printed": printed, "namelists": namelists}, fh, indent=1)
 
     # var.dat of a sample run, read by the reference's record reader
     ff = load_fortran_file_module(ref_root)
@@ -212,4 +217,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PENCIL_REFERENCE")
+    if not ref:
+        sys.exit("usage: gen_golden.py <path of the pencil-code tree> (or set PENCIL_REFERENCE)")
+    main(ref)

@@ -152,6 +152,85 @@ def test_diagnostics_fp64(pc, ic, orc):
         assert abs(got - ref) <= TOLDIAG * max(abs(ref), 1e-300), (k, got, ref)
 
 
+@pytest.mark.parametrize("mode", ["f64", "dfloat", "f32pair"])
+def test_isothermal_diagnostic_series_100_steps(pc, ic, orc, mode):
+    """The 32^3 isothermal case (noise 1e-3 from a seed, nu=eta=5e-3, dt=5e-3) with the
+    diagnostics of every step over the 100-step run -- urms, umax, brms, bmax, ekin, rhom,
+    jrms, abm, evaluated on the pre-update f of substep 1 (diagnostics.f90:274) -- against
+    the oracle's series: 1e-12 relative for the FP64-class states, 1e-5 for FP32 (abm,
+    which changes sign, relative to rms(A) brms)."""
+    kw = dict(f64=dict(precision=8), dfloat=dict(precision=8, dfloat=1),
+              f32pair=dict(precision=4, comp=1, tile=5))[mode]
+    tol = 1e-5 if mode == "f32pair" else TOLDIAG
+    p = iso_params(pc, diag_every=1, **kw)
+    f0 = iso_state(pc, ic, p)
+    box = pc.Box(p)
+    box.load(f0)
+    op = oracle_params(orc, p)
+    f = np.array(f0, order="F", copy=True)
+    df = np.zeros_like(f)
+    t = 0.0
+    nw = p.nx * p.ny * p.nz
+    worst = {}
+    for it in range(100):
+        box.steps(1)
+        got = pc.diag_summary(box.diag_raw(), nw)
+        orc.ghosts(op, f)
+        arms = np.sqrt(np.mean(f[3:-3, 3:-3, 3:-3, 4:7] ** 2) * 3)
+        t, _, dg = orc.time_step(op, f, df, t, p.dt, False, diag=True, nthreads=8)
+        ref = orc.diag_summary(op, dg)
+        for key in ("urms", "umax", "brms", "bmax", "ekin", "rhom", "jrms", "abm"):
+            # <A.B> changes sign; its sum's round-off scales with arms * brms
+            scale = arms * ref["brms"] if key == "abm" else abs(ref[key])
+            e = abs(got[key] - ref[key]) / scale
+            worst[key] = max(worst.get(key, 0.0), e)
+            assert e <= tol, (it, key, got[key], ref[key])
+        # div B is round-off in both codes: compare it with the current density
+        assert got["divbrms"] <= (1e-5 if mode == "f32pair" else 1e-12) * ref["jrms"]
+        assert ref["divbrms"] <= 1e-12 * ref["jrms"]
+    print(mode, {k: f"{v:.1e}" for k, v in worst.items()})
+
+
+def _printed_unit(text):
+    mant, _, exp = text.upper().partition("E")
+    return 10.0 ** (int(exp or 0) - (len(mant.split(".")[1]) if "." in mant else 0))
+
+
+@pytest.mark.parametrize("mode", ["f64", "dfloat", "f32pair"])
+def test_mhd_abcforcing_sample_known_answer(pc, orc, mode):
+    """samples/MHD-ABCforcing run on the GPU: 32^3 isothermal MHD, ABC forcing of uu
+    (ampl 1e-4, k=1), B_ext=(0,0.1,0), nu=eta=0.1, CFL dt of the current state with
+    cdt=0.4, 51 steps from the sample's Gaussian noise realisation (seed -10). Every
+    printed row of t, dt, urms, umax, brms, abm and epsM in the sample's reference.out
+    is met at 1.5 units of its last printed digit, in every state mode."""
+    import json
+    import os
+    ref = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "mhd_abcforcing_ref.json")))
+    prm = ref["params"]
+    kw = dict(f64=dict(precision=8), dfloat=dict(precision=8, dfloat=1),
+              f32pair=dict(precision=4, comp=1, tile=5))[mode]
+    p = pc.default_params(nx=32, ny=32, nz=32, gamma=1.0, nu=prm["nu"], eta=prm["eta"], lforcing_cont=1,
+                          ampl_ff=prm["ampl_ff"], kf=prm["k1_ff"], b_ext=tuple(prm["b_ext"]), cdt=prm["cdt"],
+                          dt=0.0, dt_mode=2, diag_every=1, **kw)
+    op = oracle_params(orc, p)
+    f0 = orc.empty_f(op)
+    orc.gaunoise_volume(op, prm["amplaa"], f0, 4, 6, -10)   # seed(1) = -10, start.f90:388
+    box = pc.Box(p)
+    box.load(f0)
+    rows = {int(r["it"]): r for r in ref["printed"]}
+    t0 = 0.0
+    for it in range(prm["nt"]):
+        box.steps(1)
+        if it in rows:
+            s = pc.diag_summary(box.diag_raw(), 32 ** 3)
+            t, dt, _ = box.time()
+            got = dict(s, t=t0, dt=dt, epsM=prm["eta"] * s["jrms"] ** 2)
+            for c in ("t", "dt", "urms", "umax", "brms", "abm", "epsM"):
+                r = rows[it][c]
+                assert abs(got[c] - float(r)) <= 1.5 * _printed_unit(r), (mode, it, c, got[c], r)
+        t0 = box.time()[0]
+
+
 @pytest.mark.parametrize("tile", [0, 4, 5, 6, 7])
 def test_isothermal_fp32_compensated(pc, ic, orc, tile):
     """FP32 state with the compensated 2N accumulation, within 1e-5 of the FP64 oracle,
