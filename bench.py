@@ -57,13 +57,19 @@ def measured_peak_hbm():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def bytes_per_cell_substep(nf: int, precision: int, comp: bool) -> float:
-    """Algorithmic HBM bytes per interior cell and substep.
+def bytes_per_cell_substep(nf: int, precision: int) -> float:
+    """Algorithmic HBM bytes per interior cell and substep, the roofline basis: read f,
+    write f, read df, write df on every substep except the first, where alpha = 0 and df
+    need not be read -- 3 nf s on substep 1 and 4 nf s on substeps 2 and 3, mean 11/3 nf s
+    (s = 4 for FP32, 8 for FP64; a double-float state is FP64-sized).  Compensation carries,
+    ghost re-reads and reductions are overhead, not algorithmic bytes."""
+    return 11.0 / 3.0 * nf * precision
 
-    FP32 compensated: read f, read df/carry, write df/carry, write f on every substep: 4*nf*4.
-    FP64 (and FP32 without compensation): substep 1 reads f, writes df and f (3 nf);
-    substep 2 reads f and df, writes both (4 nf); substep 3 reads f and df, writes f (3 nf,
-    df is dead after the last substep): mean 10/3 * nf * s."""
+
+def bytes_moved_per_cell_substep(nf: int, precision: int, comp: bool) -> float:
+    """What the kernel must move at least, overhead included: the FP32 compensated state
+    reads and writes its df/carry slot on every substep (4 nf s); FP64 substep 3 does not
+    write the dead df (mean 10/3 nf s)."""
     if precision == 4 and comp:
         return 4.0 * nf * 4
     return 10.0 / 3.0 * nf * precision
@@ -323,21 +329,28 @@ def run_ours(args):
     # the timing-run physics adds a CFL pass and the two forcing kernels per step,
     # charged here to the substeps (a lower bound on the substep kernel's rate)
     per_launch_ms = ms / (3 * args.steps)
-    bpc = bytes_per_cell_substep(nf, prec, True)
+    bpc = bytes_per_cell_substep(nf, prec)
     achieved = bpc * cells / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
-    traffic = None
+    traffic, traffic_note = None, None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         try:
             tj = json.load(open(tpath))
-            key = f"f{8 * prec}_{nf}"
-            if key in tj:
+            key = f"f{8 * prec}_{nf}{'_dd' if args.dfloat else ''}"
+            if key in tj and not timings:
                 traffic = tj[key]["bytes_per_cell_substep"] * cells
+                traffic_note = (f"dram bytes of one ncu capture ({tj[key]['file']}) scaled per cell to "
+                                f"this launch's {n}^3 cells")
         except Exception:
             traffic = None
     box.close()
     del box
+
+    # ---- FP64-class companions of the headline (512^3, same physics) ----
+    fp64_class = None
+    if not timings and not args.no_fp64_class and rank == 0 and ws == 1:
+        fp64_class = run_fp64_class(args, pc, torch, stream, peak, peak_kind)
 
     # ---- e2e through the plug-in C ABI with pinned host buffers ----
     e2e = None
@@ -376,15 +389,59 @@ def run_ours(args):
                        "parallelism": f"replicas x{ws}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "bytes_per_cell_substep": bpc},
+                         "bytes_per_cell_substep": bpc,
+                         "bytes_moved_per_cell_substep": bytes_moved_per_cell_substep(nf, prec, True),
+                         "traffic_basis": traffic_note},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
         }
+        if fp64_class is not None:
+            line["fp64_class"] = fp64_class
         if timings:
             line["published_reference"] = TIMINGS_PUBLISHED
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def run_fp64_class(args, pc, torch, stream, peak, peak_kind) -> dict:
+    """The FP64-parity states on the 512^3 headline physics, each timed alone on the
+    device (CUDA events around K steps after W warm-up steps): the double-float state
+    (FP64-class results on the FP32 pipes) and native FP64.  HBM fraction on the
+    11/3 nf s basis with s = 8; the pipe fractions are those of the ncu captures named."""
+    pipes = {}
+    ppath = os.path.join(ROOT, "profiles", "pipes.json")
+    if os.path.exists(ppath):
+        try:
+            pipes = json.load(open(ppath))
+        except Exception:
+            pipes = {}
+    n, nf = 512, 7
+    cells = float(n) ** 3
+    steps = max(1, min(args.steps, 5))
+    out = {"workload": f"isothermal MHD {n}^3, 7 fields, headline physics, {steps} RK3 steps after "
+                       f"{args.warmup} warm-up, state {3 * nf * cells * 8 / 1e9:.1f} GB (larger than L2)"}
+    for name, dfl in (("double_float", 1), ("native_fp64", 0)):
+        p = headline_params(pc, n, 8, 0, dfl)
+        box = pc.Box(p)
+        init_headline(box, p)
+        box.steps(args.warmup)
+        box.sync()
+        ms, launches = time_box_steps(pc, torch, box, stream, steps)
+        box.sync()
+        info = box.info()
+        box.close()
+        rate = cells * 3 * steps / (ms / 1e3) / 1e9
+        achieved = bytes_per_cell_substep(nf, 8) * cells / (ms / (3 * steps) / 1e3) / 1e9
+        rec = {"value": rate, "unit": "Gcell-updates/s", "ms_per_step": ms / steps, "tile": info["tile"],
+               "hbm": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "peak_kind": peak_kind, "bytes_per_cell_substep": bytes_per_cell_substep(nf, 8)},
+               "gpu_launches": launches}
+        if name in pipes:
+            rec["compute"] = pipes[name]
+        out[name] = rec
+        torch.cuda.empty_cache()
+    return out
 
 
 def _ck(L, rc: int) -> None:
@@ -462,7 +519,11 @@ def run_e2e(args, pc, gpu, torch, stream, p, nf, ws: int = 1, kvec=None):
             "h2d_bytes_per_step": ws * nbytes / args.steps,
             "d2h_bytes_per_step": ws * (nbytes / args.steps + red.nbytes),
             "what": "loadFarray + K x (substepGPU x3 + getGPUReducedVars) + copyFarray, pinned host f-array "
-                    f"(REAL={'float, libpcgb300_sgl.so' if single else 'double, libpcgb300.so'}), wall clock"}
+                    f"(REAL={'float, libpcgb300_sgl.so' if single else 'double, libpcgb300.so'}), wall clock",
+            "amortisation": f"one host-to-device load and one device-to-host copy of the whole f-array "
+                            f"({nbytes / 1e9:.1f} GB each) per {args.steps} steps, as the plug-in moves f only "
+                            f"at start-up, diagnostics and snapshots (equ.f90:307-312); the reduced "
+                            f"diagnostics come back every step"}
 
 
 def run_ensemble(args):
@@ -567,6 +628,8 @@ def main():
     ap.add_argument("--zdepth", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64-class", action="store_true",
+                    help="skip the 512^3 double-float and native FP64 companions of the headline line")
     ap.add_argument("--cpu-sample-n", type=int, default=96)
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
     ap.add_argument("--workload", default="headline", choices=["headline", "timings", "ensemble", "serve"])

@@ -174,7 +174,19 @@ void getGPUReducedVars(REAL_PCGB* dst);
 void testBCs(void);
 /* gpu_astaroth_ansi.c:44 -- split updates are not part of this path (no-op). */
 void splitUpdate(const REAL_PCGB eps, const int max_iter);
-/* gpu_astaroth_ansi.c:45 -- device pointers of the input and output f buffers. */
+/* gpu_astaroth_ansi.c:45 -- device pointers of the input and output f buffers.
+   They point at this library's device layout, not at the reference's field
+   buffers of stride mw = mx*my*mz (gpu_astaroth.cc:1833-1848): element
+   (i, j, k, slice), interior i in [0,nx), sits at
+     slice*fs + (k+3)*ps + (j+3)*px + xoff + i
+   with xoff, px, ps = px*(ny+6), fs = ps*(nz+6) as pcgb_box_info reports them,
+   and the element is the device state's type whatever REAL_PCGB is: float for
+   precision 4, double for precision 8, a 16-byte (hi_a, hi_b, lo_a, lo_b) float
+   quadruple for the double-float state.  Field-major tiles (0-3) hold one
+   slice per field in f-array order; the pair tiles (4-7 of the FP32 and
+   double-float states) hold four slices of field pairs (ux,ax) (uy,ay) (uz,az)
+   (lnrho, ss or 0), interleaved per element.  copyFarray gives the reference
+   layout on the host. */
 void copyVBApointers(REAL_PCGB** in, REAL_PCGB** out);
 
 /* gpu_astaroth_ansi.c:48-56 -- TorchFort hooks: not part of this path (no-ops). */
@@ -334,10 +346,14 @@ int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, double* ms_per_s
  * periodic ghosts (every f_out written by this call does).  One call performs
  * substep isubstep (1..3) of the 2N-RK3 scheme with timestep dt (FP64 or FP32
  * state, without the FP32 carry): df is written on substeps 1-2 and read on
- * 2-3.  If reductions != NULL (host array of PCGB_NSLOT doubles) the call waits
- * for the kernel and returns, on substep 1, the CFL inverse timestep in [0]
- * and the diagnostic slots (sums/maxima of u^2, B^2, ...) in [1..9].
- * stream is a cudaStream_t (NULL: the default stream).
+ * 2-3.  If reductions != NULL (host array of PCGB_NOALLOC_NRED doubles) the
+ * call waits for the kernel and returns, on substep 1, the CFL inverse
+ * timestep in [0] and the diagnostic slots (sums/maxima of u^2, B^2, ...) in
+ * [1..9]; only such a call reads back the kernel's error flags (return 5).  A
+ * call without reductions returns once its kernel is queued.  The parameter
+ * block is checked as pcgb_box_create checks it.  Each call uploads its
+ * descriptor, step state and forcing tables with cudaMemcpyAsync from host
+ * memory of the call.  stream is a cudaStream_t (NULL: the default stream).
  *
  * Its scratch (descriptor, step state, forcing tables, per-tile partials) is
  * a fixed file-scope device array of about 1.5 MB that every GPU using the
@@ -349,6 +365,7 @@ int pcgb_autotune(const pcgb_params* p, int* tile, int* zdepth, double* ms_per_s
  * error flag). */
 #define PCGB_NOALLOC_MAX_EXTENT 4096
 #define PCGB_NOALLOC_MAX_TILES 16384
+#define PCGB_NOALLOC_NRED 10   /* doubles in the reductions array */
 int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double dt, const void* f_in, void* f_out, void* df,
                          double* reductions, void* stream);
 

@@ -19,9 +19,16 @@
 //
 // Every call reuses the same scratch and leaves the last call's contents in
 // it; each call rewrites the descriptor, the state (including the tile
-// counter that must start at zero) and the forcing tables before launching.
-// Calls whose kernels overlap on the GPU (several streams, or several host
-// threads) race on the scratch and must be serialised by the caller.
+// counter that must start at zero) and the forcing tables before launching,
+// by cudaMemcpyAsync from host memory of the call.  Calls whose kernels
+// overlap on the GPU (several streams, or several host threads) race on the
+// scratch and must be serialised by the caller.
+//
+// Device-side errors (a bounded wait that ran out, a non-finite state) are
+// read back only by a call given a reductions array: such a call waits for
+// its kernel and returns 5 when the kernel flagged one.  A call without
+// reductions returns as soon as its kernel is queued, and the next call's
+// state upload clears the flags.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
@@ -33,6 +40,7 @@
 #include "boundcond.h"
 #include "../../include/pcgb300.h"
 #include "kernels.cuh"
+#include "params_check.h"
 #include "pcgb_box.h"
 
 using namespace pcgb;
@@ -65,13 +73,17 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
                                     void* df, double* reductions, void* stream) {
   if (!p || !f_in || !f_out || !df || isubstep < 1 || isubstep > 3 || !(dt > 0.0))
     return fail(2, "invalid argument");
-  if (p->precision != 4 && p->precision != 8) return fail(2, "precision must be 4 or 8");
+  if (p->nx > kMaxExtent || p->ny > kMaxExtent || p->nz > kMaxExtent)
+    return fail(7, "grid extent above PCGB_NOALLOC_MAX_EXTENT");
+  {
+    char buf[160];
+    const char* msg = params_problem(p, buf, sizeof(buf));   // the box path's checks
+    if (msg) return fail(2, msg);
+  }
   if (p->dfloat) return fail(2, "double-float state is not available here (use the box API)");
   if (p->lforcing_hel) return fail(2, "the step-end helical forcing is applied by the box API only");
   for (int d = 0; d < 3; ++d)
     if (!axis_periodic(*p, d)) return fail(2, "non-periodic boundaries are applied by the box API only");
-  if (p->nx < 6 || p->ny < 6 || p->nz < 6 || p->nx > kMaxExtent || p->ny > kMaxExtent || p->nz > kMaxExtent)
-    return fail(7, "grid extent outside [6, PCGB_NOALLOC_MAX_EXTENT]");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   // set-up once per device, with the device current
@@ -193,8 +205,11 @@ extern "C" int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double d
 
   LaunchArgs a;
   a.boxes = d_desc; a.nboxes = 1; a.total_tiles = h.tiles; a.work_counter = nullptr;
-  a.mode = MODE_SUBSTEP; a.wait_limit = 1u << 26; a.inject_wait_failure = 0;
+  a.mode = MODE_SUBSTEP; a.wait_limit = current_wait_limit(); a.inject_wait_failure = 0;
   void* args[] = {&a};
+  // the dynamic shared-memory allowance is an attribute of the current device's context
+  if (cudaFuncSetAttribute(kh.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kh.smem) != cudaSuccess)
+    return fail(1, "cudaFuncSetAttribute failed");
   if (cudaLaunchKernel(kh.fn, dim3(h.tiles), dim3(kh.threads), args, (size_t)kh.smem, s) != cudaSuccess)
     return fail(1, "kernel launch failed");
   if (reductions) {

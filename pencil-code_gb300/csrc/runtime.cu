@@ -29,6 +29,7 @@
 #include "boundcond.h"
 #include "cfl_pair.h"
 #include "helical.h"
+#include "params_check.h"
 #include "kernels.cuh"
 #include "pcgb_box.h"
 
@@ -331,42 +332,13 @@ static void box_free(pcgb_box* b) {
 }
 
 static int validate(const pcgb_params* p) {
-  if (!p) return set_err(PCGB_E_ARG, "null parameter block");
-  // >= 2 x nghost cells: the substep kernel writes each cell's periodic ghost
-  // image on one side of an axis (Images in mhd_common.cuh)
-  if (p->nx < 6 || p->ny < 6 || p->nz < 6)
-    return set_err(PCGB_E_ARG, "grid %dx%dx%d: each axis needs >= 6 cells", p->nx, p->ny, p->nz);
-  if (p->precision != 4 && p->precision != 8) return set_err(PCGB_E_ARG, "precision must be 4 or 8");
-  if (p->dfloat != 0 && p->dfloat != 1) return set_err(PCGB_E_ARG, "dfloat must be 0 or 1");
-  if (p->dfloat && p->precision != 8) return set_err(PCGB_E_ARG, "dfloat needs precision 8 (FP64-class state)");
-  if (!(p->Lxyz[0] > 0 && p->Lxyz[1] > 0 && p->Lxyz[2] > 0)) return set_err(PCGB_E_ARG, "Lxyz must be positive");
-  if (!(p->cs0 > 0 && p->rho0 > 0 && p->cp > 0 && p->gamma > 0 && p->mu0 > 0))
-    return set_err(PCGB_E_ARG, "cs0, rho0, cp, gamma, mu0 must be positive");
-  if (!(p->cdt > 0 && p->cdtv > 0)) return set_err(PCGB_E_ARG, "cdt and cdtv must be positive");
-  if (p->dt < 0) return set_err(PCGB_E_ARG, "dt must be >= 0");
-  if (p->lforcing_hel != 0 && p->lforcing_hel != 1) return set_err(PCGB_E_ARG, "lforcing_hel must be 0 or 1");
-  if (p->lforcing_hel && !(p->force_hel >= 0.0)) return set_err(PCGB_E_ARG, "force_hel must be >= 0");
-  if (p->lmagnetic_forcing != 0 && p->lmagnetic_forcing != 1) return set_err(PCGB_E_ARG, "lmagnetic_forcing must be 0 or 1");
-  if (p->lmagnetic_forcing && !p->lforcing_hel)
-    return set_err(PCGB_E_ARG, "lmagnetic_forcing applies to random helical forcing (lforcing_hel)");
-  if ((p->lupw_uu != 0 && p->lupw_uu != 1) || (p->lupw_lnrho != 0 && p->lupw_lnrho != 1))
-    return set_err(PCGB_E_ARG, "lupw_uu and lupw_lnrho must be 0 or 1");
-  const int nf = params_nf(*p);
-  for (int d = 0; d < 3; ++d) {
-    int nper = 0;
-    for (int k = 0; k < nf; ++k)
-      for (int side = 0; side < 2; ++side) {
-        const int c = p->bc[d][k][side];
-        if (c < PCGB_BC_PER || c > PCGB_BC_ASYM2)
-          return set_err(PCGB_E_ARG, "boundary condition code %d (direction %d, field %d) is not one of p, s, a, a2",
-                         c, d, k);
-        nper += (c == PCGB_BC_PER);
-      }
-    if (nper != 0 && nper != 2 * nf)
-      return set_err(PCGB_E_ARG, "direction %d mixes periodic and non-periodic boundary conditions", d);
-  }
-  return 0;
+  char buf[160];
+  const char* msg = params_problem(p, buf, sizeof(buf));
+  return msg ? set_err(PCGB_E_ARG, "%s", msg) : 0;
 }
+
+// The wait limit the box path uses, for the allocation-free entry point.
+unsigned int pcgb::current_wait_limit() { return g.wait_limit; }
 
 extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   std::lock_guard<std::mutex> lk(g_mu);

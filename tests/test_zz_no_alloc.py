@@ -103,3 +103,57 @@ def test_noalloc_rejects_oversize(pc):
     assert L.pcgb_substep_noalloc(C.byref(p), 1, 1e-3, dummy, dummy, dummy, None, None) == 7
     p = pc.default_params(nx=32, ny=32, nz=32, precision=8, dt=1e-3)
     assert L.pcgb_substep_noalloc(C.byref(p), 4, 1e-3, dummy, dummy, dummy, None, None) == 2
+
+
+def test_noalloc_fp32_plain_2n_against_oracle(pc, ic, orc):
+    """FP32 state through the allocation-free entry: it runs the plain 2N update
+    (the compensated carry would need state kept between calls), so its error is
+    stated against the FP64 oracle: 20 RK3 steps of the 32^3 isothermal case
+    (noise 1e-3 plus an ABC flow of 0.1) within 1e-5 per field, lnrho measured
+    against max(|lnrho|, 1).  Calls after the first allocate no device memory:
+    the device's free memory and torch's allocation count do not change."""
+    torch = pytest.importorskip("torch")
+    from conftest import LOG7, oracle_params
+    L = pc.load()
+    n, steps, dt = 32, 20, 5e-3
+    p = pc.default_params(nx=n, ny=n, nz=n, gamma=1.0, nu=5e-3, eta=5e-3, dt=dt, precision=4, comp=0, tile=0)
+    f0 = ic.zeros(p)
+    ic.gaussian_noise(f0, p, ["ux", "uy", "uz", "ax", "ay", "az"], 1e-3, 1)
+    ic.abc_flow(f0, p, ampl=0.1)
+    ic.fill_ghosts(f0)
+    xoff = 128 // 4
+    px = xoff + ((p.nx + 8 + xoff - 1) // xoff) * xoff
+    mx = p.nx + 6
+    a = torch.from_numpy(to_device_layout(f0, xoff, px).astype(np.float32)).cuda()
+    b = torch.zeros_like(a)
+    df = torch.zeros_like(a)
+    bufs = [a, b]
+    torch.cuda.synchronize()
+    rc = L.pcgb_substep_noalloc(C.byref(p), 1, dt, C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+                                C.c_void_p(df.data_ptr()), None, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    allocs0 = torch.cuda.memory_stats().get("allocation.all.allocated", 0)
+    k = 1   # the first substep above wrote bufs[1]
+    for it in range(3 * steps - 1):
+        s = (it + 1) % 3 + 1
+        src, dst = bufs[k], bufs[k ^ 1]
+        rc = L.pcgb_substep_noalloc(C.byref(p), s, dt, C.c_void_p(src.data_ptr()), C.c_void_p(dst.data_ptr()),
+                                    C.c_void_p(df.data_ptr()), None, None)
+        assert rc == 0
+        k ^= 1
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_stats().get("allocation.all.allocated", 0) == allocs0
+    g = from_device_layout(bufs[k].cpu().numpy().astype(np.float64), xoff, mx)
+    op = oracle_params(orc, p)
+    ref = np.array(f0, order="F", copy=True)
+    dref = np.zeros_like(ref)
+    t = 0.0
+    for _ in range(steps):
+        t, _, _ = orc.time_step(op, ref, dref, t, dt, False, nthreads=8)
+    orc.ghosts(op, ref)
+    err = rel_err(g, ref, LOG7)
+    print("noalloc FP32 plain 2N, 20 steps:", [f"{e:.2e}" for e in err])
+    assert np.all(err <= 1e-5), err
