@@ -630,8 +630,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-class", action="store_true",
                     help="skip the 512^3 double-float and native FP64 companions of the headline line")
-    ap.add_argument("--cpu-sample-n", type=int, default=96)
-    ap.add_argument("--cpu-sample-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample-n", type=int, default=160)
+    ap.add_argument("--cpu-sample-steps", type=int, default=60)
     ap.add_argument("--workload", default="headline", choices=["headline", "timings", "ensemble", "serve"])
     ap.add_argument("--boxes", type=int, default=192)
     ap.add_argument("--seed", type=int, default=0)

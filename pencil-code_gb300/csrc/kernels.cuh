@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include "cell_ddpair.cuh"
 #include "cell_pair.cuh"
+#include "cell_pair_tmem.cuh"
 #include "cell_scalar.cuh"
 #include "mhd_driver.cuh"
 
@@ -10,7 +11,9 @@ namespace pcgb {
 
 // Tile variants.  Ids 0..3 use the field-major layout (one value per field per
 // cell); for FP32 and double-float, ids 4..7 use the packed field-pair layout
-// (cell_pair.cuh: float2 elements; cell_ddpair.cuh: 16-byte dd2 elements).
+// (cell_pair.cuh: float2 elements; cell_ddpair.cuh: 16-byte dd2 elements).  The
+// default FP32 pair tile 5 keeps its z-direction data in tensor memory
+// (cell_pair_tmem.cuh); its upwinding variant is the shared-memory PairCell.
 //   FP32: 0 (32,4)x2  1 (32,8)  2 (16,8)x2  3 (64,4)  4 pair(32,4)x2  5 pair(32,8)  6 pair(16,8)x2  7 pair(64,4)
 //   FP64: 0 (32,4)  1 (16,8)  2 (24,8)  3 (32,6)
 //   double-float: 0..3 as FP64, 4 pair(24,8)  5 pair(16,12)  6 pair(16,8)  7 pair(32,4)
@@ -120,7 +123,7 @@ static KernelHandle make_kernel_handle() {
           case 2: cache[2] = make_kernel_handle<ScalarCell<T, NF, 16, 8>, 16, 8, 9, 2>(); break;   \
           case 3: cache[3] = make_kernel_handle<ScalarCell<T, NF, 64, 4>, 64, 4, 9, 1>(); break;   \
           case 4: cache[4] = make_kernel_handle<PairCell<NF, 32, 4>, 32, 4, 8, 2>(); break;        \
-          case 5: cache[5] = make_kernel_handle<PairCell<NF, 32, 8>, 32, 8, 9, 1>(); break;        \
+          case 5: cache[5] = make_kernel_handle<PairCellTM<NF, 32, 8>, 32, 8, 9, 1>(); break;      \
           case 6: cache[6] = make_kernel_handle<PairCell<NF, 16, 8>, 16, 8, 8, 2>(); break;        \
           default: cache[7] = make_kernel_handle<PairCell<NF, 64, 4>, 64, 4, 8, 1>(); break;       \
         }                                                                                          \

@@ -34,6 +34,19 @@ namespace pcgb {
 // enough for any TMA load to land, so a CTA never leaves with copies pending.
 constexpr unsigned int kDrainWaitLimit = 1u << 26;
 
+// Cells that keep state in tensor memory declare kTmemCols (columns the CTA
+// allocates) and kColsPerThread; the others use none.
+template <class C, class = void>
+struct CellTmem {
+  static constexpr int cols = 0, per_thread = 0;
+  static constexpr bool whole_warp = false;
+};
+template <class C>
+struct CellTmem<C, decltype((void)C::kTmemCols, void())> {
+  static constexpr int cols = C::kTmemCols, per_thread = C::kColsPerThread;
+  static constexpr bool whole_warp = C::kWholeWarp;
+};
+
 template <class CELL, int TX, int TY, int RING>
 struct DriverCfg {
   using Elem = typename CELL::Elem;
@@ -70,13 +83,28 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
   const int tx = tid % TX, ty = tid / TX;
   const int lane = tid & 31, warp = tid >> 5;
 
+  constexpr int TMC = CellTmem<CELL>::cols;
+  if constexpr (TMC > 0) {
+    if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh[2])),
+                   "n"(TMC) : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+  }
   if (tid == 0) {
     for (int r = 0; r <= RING; ++r) mbar_init(&full[r], 1);   // full[RING]: never arrived on
     for (int r = 0; r < RING; ++r) released[r] = 0u;
     *abort_flag = 0;
     fence_mbar_init();
   }
+  if constexpr (TMC > 0) asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  uint32_t tm_thread = 0;
+  if constexpr (TMC > 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tm_thread = (uint32_t)sh[2] + ((uint32_t)(32 * (warp & 3)) << 16) +
+                (uint32_t)((warp >> 2) * CellTmem<CELL>::per_thread);
+  }
 
   unsigned int gplane = 0;   // planes loaded by this CTA in this launch (ring slot and phase tracking)
   int iter = 0;
@@ -164,19 +192,32 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
     const bool active = (x < B.nx) && (y < B.ny);
     typename CELL::Tile cell;
     cell.begin(B, inb, x, y, z0, active, mode_cfl, fl);
+    if constexpr (TMC > 0) { cell.tm = tm_thread; cell.zfirst = z0; }
+    const bool warp_live = __any_sync(0xffffffffu, active);
 
     Acc acc;
     acc.reset();
     T dt1max = T(0);
 
+    // rolling ring positions: ws/wp = slot and phase of plane j+6 (the newest this
+    // output needs), rs = slot of plane j (released after it), po = offsets of the
+    // seven planes z-3..z+3 of this thread's column
+    unsigned int ws = 0u, wp = 0u, rs = sbase;
+    unsigned int po[7];
     for (int z = z0; z < z1; ++z) {
       const int j = z - z0;
-      // wait for planes j..j+6 (only the newest is new after the first plane)
-      const int jw0 = (j == 0) ? 0 : j + 6;
       int lfail = 0;
-      for (int jw = jw0; jw <= j + 6; ++jw) {
-        const unsigned int r = sbase + (unsigned int)jw;
-        if (!mbar_wait_bounded(&full[r % RING], ((r / RING) + pbase) & 1u, args.wait_limit)) lfail = 1;
+      if (j == 0) {
+        for (int jw = 0; jw <= 6; ++jw) {
+          const unsigned int r = sbase + (unsigned int)jw;
+          if (!mbar_wait_bounded(&full[r % RING], ((r / RING) + pbase) & 1u, args.wait_limit)) lfail = 1;
+        }
+        const unsigned int r6 = sbase + 6u;
+        ws = r6 % RING;
+        wp = ((r6 / RING) + pbase) & 1u;
+      } else {
+        if (++ws == (unsigned int)RING) { ws = 0u; wp ^= 1u; }
+        if (!mbar_wait_bounded(&full[ws], wp, args.wait_limit)) lfail = 1;
       }
       // failure-detection test hook: a flag that nothing sets, waited for with the same bound
       if (args.inject_wait_failure && !mbar_wait_bounded(&full[RING], 0u, args.wait_limit)) lfail = 1;
@@ -187,23 +228,33 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
         break;
       }
 
-      if (active) {
-        const Elem* pl[7];
-        const unsigned int s0 = (sbase + (unsigned int)j) % RING;
-        const unsigned char* cbase = smem + ((ty + 3) * C::BW + (tx + 4)) * (int)sizeof(Elem);
+      if (CellTmem<CELL>::whole_warp && !mode_cfl ? warp_live : active) {
+        if (j == 0) {
+          const unsigned int cb = ((ty + 3) * C::BW + (tx + 4)) * (int)sizeof(Elem);
 #pragma unroll
-        for (int d = 0; d < 7; ++d) {
-          const unsigned int sd = (s0 + d >= (unsigned int)RING) ? s0 + d - RING : s0 + d;
-          pl[d] = reinterpret_cast<const Elem*>(cbase + sd * C::SLOT_BYTES);
+          for (int dd = 0; dd < 7; ++dd) po[dd] = cb + ((sbase + dd) % RING) * C::SLOT_BYTES;
+        } else {
+#pragma unroll
+          for (int dd = 0; dd < 6; ++dd) po[dd] = po[dd + 1];
+          const unsigned int n6 = po[5] + C::SLOT_BYTES;
+          po[6] = n6 >= (unsigned int)(RING * C::SLOT_BYTES) ? n6 - RING * C::SLOT_BYTES : n6;
         }
-        if (!mode_cfl) cell.step(pl, x, y, z, z1, fl, acc, dt1max);
-        else cell.cfl(pl, dt1max);
+        const Elem* pl[7];
+#pragma unroll
+        for (int dd = 0; dd < 7; ++dd) pl[dd] = reinterpret_cast<const Elem*>(smem + po[dd]);
+        if constexpr (CellTmem<CELL>::whole_warp) {
+          if (!mode_cfl) cell.step(pl, x, y, z, z1, fl, acc, dt1max, active);
+          else cell.cfl(pl, dt1max);
+        } else {
+          if (!mode_cfl) cell.step(pl, x, y, z, z1, fl, acc, dt1max);
+          else cell.cfl(pl, dt1max);
+        }
       }
 
       // this warp is done with ring plane j; the last warp to say so refills its slot
       __syncwarp();
       if (lane == 0) {
-        const unsigned int slot = (sbase + (unsigned int)j) % RING;
+        const unsigned int slot = rs;
         __threadfence_block();
         const unsigned int prev = atomicAdd(&released[slot], 1u);
         if (prev == (unsigned int)(C::NWARP - 1)) {
@@ -217,6 +268,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
           }
         }
       }
+      rs = (rs + 1u == (unsigned int)RING) ? 0u : rs + 1u;
     }
     failed = __syncthreads_or(failed);
     if (failed && tid == 0) {
@@ -316,6 +368,14 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
       }
     }
     __syncthreads();
+  }
+  if constexpr (TMC > 0) {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"((uint32_t)sh[2]), "n"(TMC)
+                   : "memory");
   }
 }
 
