@@ -352,6 +352,15 @@ def run_ours(args):
     if not timings and not args.no_fp64_class and rank == 0 and ws == 1:
         fp64_class = run_fp64_class(args, pc, torch, stream, peak, peak_kind)
 
+    # ---- ensemble and serving companions (rank 0, N=1) ----
+    ensemble = serving = None
+    if not timings and rank == 0 and ws == 1 and not args.no_ensemble:
+        ensemble = ensemble_measure(pc, torch, stream, 192, 5, 3, 5, 500, args.seed, quick=True)
+        L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
+    if not timings and rank == 0 and ws == 1 and not args.no_serve:
+        serving = serve_measure(pc, 24, [5.0, 50.0], 0.1, 0.5, False, 150.0, 10, args.seed)
+        L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
+
     # ---- e2e through the plug-in C ABI with pinned host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -396,6 +405,10 @@ def run_ours(args):
         }
         if fp64_class is not None:
             line["fp64_class"] = fp64_class
+        if ensemble is not None:
+            line["ensemble"] = ensemble
+        if serving is not None:
+            line["serving"] = serving
         if timings:
             line["published_reference"] = TIMINGS_PUBLISHED
         print(json.dumps(line), flush=True)
@@ -526,20 +539,20 @@ def run_e2e(args, pc, gpu, torch, stream, p, nf, ws: int = 1, kvec=None):
                             f"diagnostics come back every step"}
 
 
-def run_ensemble(args):
-    """Ensemble workload: args.boxes boxes of uneven sizes and parameters, args.steps RK3 steps
-    each, batched persistent launches under CUDA-graph replay vs the single-box kernel looping
-    over the boxes.  Both legs advance every box by the same number of steps."""
-    import torch
-    pc = importlib.import_module("pencil-code_gb300")
+def ensemble_measure(pc, torch, stream, boxes_n: int, steps: int, warmup: int, graph_steps: int, solve_steps: int,
+                     seed: int = 0, quick: bool = False) -> dict:
+    """Ensemble workload: boxes_n boxes of uneven sizes and parameters, `steps` RK3 steps each,
+    batched persistent launches under CUDA-graph replay (tile from the batched autotuner, z-depth
+    per box size) against the single-box kernel looping over the boxes with its defaults.  Both
+    legs advance every box by the same number of steps; solves/s scales the timed steps to a
+    solve of solve_steps steps."""
     ens = importlib.import_module("pencil-code_gb300.ensemble")
     L = pc.load()
-    stream = torch.cuda.Stream()
-    L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
-    specs = ens.make_ensemble(args.boxes, seed=args.seed)
+    specs = ens.make_ensemble(boxes_n, seed=seed)
     cells = sum(p.nx * p.ny * p.nz for p, _ in specs)
-    # batched leg: tile and z-depth from the batched autotuner; plain leg: single-box defaults
-    t_tile, t_zd, table = ens.autotune_batch(specs)
+    kw = dict(tiles=(5, 6), zdepths=(32, 64), per_size_zdepths=(16, 32, 64, 128), sample=12,
+              per_size_sample=4) if quick else {}
+    t_tile, t_zd, table = ens.autotune_batch(specs, **kw)
     tuned = ens.with_tiling(specs, t_tile, t_zd)
     out = {}
     for leg in ("batched", "plain"):
@@ -547,68 +560,95 @@ def run_ensemble(args):
         torch.cuda.synchronize()
         if leg == "batched":
             batch = pc.Batch(boxes, persistent=True)
-            batch.steps(args.warmup, use_graph=False)
+            batch.steps(warmup, use_graph=False)
         else:
             for b in boxes:
-                b.steps(args.warmup)
+                b.steps(warmup)
         torch.cuda.synchronize()
         n0 = L.pcgb_launch_count()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         if leg == "batched":
-            batch.steps(args.steps, use_graph=True, graph_steps=args.graph_steps)
+            batch.steps(steps, use_graph=True, graph_steps=graph_steps)
         else:
             for b in boxes:
-                b.steps(args.steps)
+                b.steps(steps)
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         for b in boxes:
             b.sync()
-        out[leg] = {"ms": ms, "solves_per_s": len(boxes) * args.steps / args.solve_steps / (ms / 1e3),
-                    "gcell_per_s": cells * 3 * args.steps / (ms / 1e3) / 1e9,
+        out[leg] = {"ms": ms, "solves_per_s": len(boxes) * steps / solve_steps / (ms / 1e3),
+                    "gcell_per_s": cells * 3 * steps / (ms / 1e3) / 1e9,
                     "launches": int(L.pcgb_launch_count() - n0)}
         if leg == "batched":
             batch.close()
         for b in boxes:
             b.close()
         torch.cuda.empty_cache()
-    line = {"metric": "ensemble solves/s", "value": out["batched"]["solves_per_s"], "unit": "solves/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-            "dtype": "f32", "data": "synthetic (seeded on device)",
-            "config": {"workload": f"{args.boxes} isothermal MHD boxes, sizes from {{32,48,64,96,128}}^3, "
-                                   f"nu,eta log-uniform [1e-3,1e-2], ABC ampl U[0.01,0.05] k in {{1,2,3}}, "
-                                   f"CFL dt cdt=0.4, FP32 state, FP64 reductions",
-                       "solve": f"{args.solve_steps} RK3 steps", "graph_steps": args.graph_steps,
-                       "autotuned": {"tile": t_tile, "zdepth": t_zd,
-                                     "ms_per_step": {f"{k[0]}/{k[1]}": round(v, 3) for k, v in table.items()}}},
+    return {"metric": "ensemble solves/s", "value": out["batched"]["solves_per_s"], "unit": "solves/s",
+            "workload": f"{boxes_n} isothermal MHD boxes, sizes from {{32,48,64,96,128}}^3, nu,eta log-uniform "
+                        f"[1e-3,1e-2], ABC ampl U[0.01,0.05] k in {{1,2,3}}, CFL dt cdt=0.4 (lagged), FP32 "
+                        f"compensated state, FP64 reductions; {steps} RK3 steps of every box timed after {warmup}, "
+                        f"scaled to solves of {solve_steps} steps",
+            "graph_steps": graph_steps,
+            "autotuned": {"tile": t_tile, "zdepth_by_size": {str(k): v for k, v in t_zd.items()},
+                          "ms_per_step": {f"{k[0]}/{k[1]}": round(v, 3) for k, v in table.items()}},
             "batched": out["batched"], "plain": out["plain"],
-            "speedup_vs_plain": out["batched"]["solves_per_s"] / out["plain"]["solves_per_s"]}
+            "speedup_vs_plain": out["batched"]["solves_per_s"] / out["plain"]["solves_per_s"],
+            "target_speedup": 4.0}
+
+
+def run_ensemble(args):
+    import torch
+    pc = importlib.import_module("pencil-code_gb300")
+    L = pc.load()
+    stream = torch.cuda.Stream()
+    L.pcgb_set_stream(C.c_void_p(stream.cuda_stream))
+    res = ensemble_measure(pc, torch, stream, args.boxes, args.steps, args.warmup, args.graph_steps,
+                           args.solve_steps, args.seed)
+    line = {"metric": res["metric"], "value": res["value"], "unit": res["unit"], "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded on device)",
+            "config": {"workload": res["workload"], "graph_steps": args.graph_steps, "autotuned": res["autotuned"]},
+            "batched": res["batched"], "plain": res["plain"], "speedup_vs_plain": res["speedup_vs_plain"]}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_serve(args):
+def serve_measure(pc, requests: int, rates, steps_scale: float, fp64_fraction: float, fp64_native: bool,
+                  budget_gb: float, round_steps: int, seed: int = 0) -> dict:
+    """The request stream served by the continuous-batching server and FIFO one at a time."""
     serve = importlib.import_module("pencil-code_gb300.serve")
-    pc = importlib.import_module("pencil-code_gb300")
     pc.load()
     res = []
-    for rate in args.rates:
-        reqs = serve.draw_requests(args.requests, seed=args.seed, steps_scale=args.steps_scale,
-                                   fp64_fraction=args.fp64_fraction, fp64_dfloat=not args.fp64_native)
+    for rate in rates:
+        reqs = serve.draw_requests(requests, seed=seed, steps_scale=steps_scale, fp64_fraction=fp64_fraction,
+                                   fp64_dfloat=not fp64_native)
         row = {"rate": rate}
         for mode, maxa in (("batched", 1 << 20), ("fifo", 1)):
-            row[mode] = serve.run_stream(reqs, rate, seed=args.seed, max_active=maxa, budget=args.budget_gb * 1e9,
-                                         round_steps=args.round_steps)
+            row[mode] = serve.run_stream(reqs, rate, seed=seed, max_active=maxa, budget=budget_gb * 1e9,
+                                         round_steps=round_steps)
+        row["p99_batched_over_fifo"] = (row["batched"]["p99_s"] / row["fifo"]["p99_s"]
+                                        if row["fifo"]["p99_s"] else None)
+        row["solves_batched_over_fifo"] = (row["batched"]["solves_per_s"] / row["fifo"]["solves_per_s"]
+                                           if row["fifo"]["solves_per_s"] else None)
         res.append(row)
-    line = {"metric": "serving solves/s and latency", "unit": "solves/s, s", "n_gpus": 1,
-            "data": "synthetic Poisson request stream",
-            "config": {"requests": args.requests, "sizes": "{32,64,128,256}^3 weights .4/.3/.2/.1",
-                       "physics": "isothermal or entropy p=0.5", "fp64_fraction": args.fp64_fraction,
-                       "fp64_state": "native FP64" if args.fp64_native else "double-float (FP64 parity bar)",
-                       "steps": f"U[100,2000] x {args.steps_scale}", "budget_gb": args.budget_gb,
-                       "round_steps": args.round_steps},
+    return {"metric": "serving solves/s and latency", "unit": "solves/s, s",
+            "config": {"requests": requests, "sizes": "{32,64,128,256}^3 weights .4/.3/.2/.1",
+                       "physics": "isothermal or entropy p=0.5", "fp64_fraction": fp64_fraction,
+                       "fp64_state": "native FP64" if fp64_native else "double-float (FP64 parity bar)",
+                       "steps": f"U[100,2000] x {steps_scale}", "budget_gb": budget_gb, "round_steps": round_steps,
+                       "scale": (f"step counts x {steps_scale} at the arrival rates as written: every request "
+                                 f"needs {steps_scale}x the work, so the offered load is {steps_scale}x config 5's")
+                       if steps_scale != 1.0 else "as written"},
             "results": res}
+
+
+def run_serve(args):
+    pc = importlib.import_module("pencil-code_gb300")
+    line = serve_measure(pc, args.requests, args.rates, args.steps_scale, args.fp64_fraction, args.fp64_native,
+                         args.budget_gb, args.round_steps, args.seed)
+    line.update({"n_gpus": 1, "data": "synthetic Poisson request stream"})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -630,6 +670,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-class", action="store_true",
                     help="skip the 512^3 double-float and native FP64 companions of the headline line")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble companion of the headline line")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving companion of the headline line")
     ap.add_argument("--cpu-sample-n", type=int, default=160)
     ap.add_argument("--cpu-sample-steps", type=int, default=60)
     ap.add_argument("--workload", default="headline", choices=["headline", "timings", "ensemble", "serve"])
@@ -638,7 +680,7 @@ def main():
     ap.add_argument("--graph-steps", type=int, default=10)
     ap.add_argument("--solve-steps", type=int, default=500)
     ap.add_argument("--requests", type=int, default=40)
-    ap.add_argument("--rates", type=float, nargs="+", default=[5.0, 50.0])
+    ap.add_argument("--rates", type=float, nargs="+", default=[5.0, 20.0, 50.0, 200.0])
     ap.add_argument("--steps-scale", type=float, default=0.1)
     ap.add_argument("--fp64-fraction", type=float, default=0.5)
     ap.add_argument("--fp64-native", action="store_true", help="serve FP64 requests with native FP64 state")

@@ -299,11 +299,16 @@ int pcgb_batch_steps(pcgb_batch* b, int nsteps, int use_graph, int graph_steps);
 
 /* Request server with continuous batching.  Requests (a parameter block,
    a step count and a seeded initial condition) are admitted in arrival order
-   while their device memory fits the budget; admitted boxes advance together,
-   one persistent launch per substep per class (precision, field count), in
-   rounds of at most round_steps RK3 steps; boxes that finish leave and
-   waiting requests join between rounds.  max_active = 1 gives FIFO
-   one-at-a-time service.  Times are seconds since the server was created. */
+   while their device memory fits the budget.  Each round advances the oldest
+   request together with the younger requests of its class (precision, field
+   count, kernel variant) that fit into the kernel waves the oldest one fills
+   alone, and, while less than one wave of the GPU is busy, younger requests of
+   other classes: one persistent launch per substep per class, the classes on
+   streams of their own, in rounds of at most round_steps RK3 steps.  Boxes that
+   finish leave and waiting requests join between rounds.  While it runs, the
+   server's thread drives the library's engine (its stream is the server's).
+   max_active = 1 gives FIFO one-at-a-time service.  Times are seconds since the
+   server was created. */
 typedef struct pcgb_server pcgb_server;
 pcgb_server* pcgb_server_create(size_t mem_budget_bytes, int max_active, int round_steps);
 /* init: Gaussian noise of amplitude noise_ampl on aa (seeded), ABC flow of

@@ -11,6 +11,10 @@ namespace pcgb {
 // Iteration limit of the kernel's bounded waits as pcgb_set_wait_limit set it
 // (defined by the runtime of each library).
 unsigned int current_wait_limit();
+// CTAs in one full wave of a box's substep kernel (occupancy x SMs).
+int box_wave(const pcgb_box* b);
+// Make s the engine's stream and return the previous one (nothing is destroyed).
+void* engine_swap_stream(void* s);
 
 // Returns nullptr when p is valid, else a message (written into buf when it
 // carries numbers).

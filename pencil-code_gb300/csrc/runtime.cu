@@ -340,6 +340,21 @@ static int validate(const pcgb_params* p) {
 // The wait limit the box path uses, for the allocation-free entry point.
 unsigned int pcgb::current_wait_limit() { return g.wait_limit; }
 
+// For the request server: CTAs of one full wave of a box's substep kernel, and
+// a stream switch that never destroys the stream it replaces.
+int pcgb::box_wave(const pcgb_box* b) {
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, b->kh.fn, b->kh.threads, (size_t)b->kh.smem) != cudaSuccess)
+    occ = 1;
+  return std::max(occ, 1) * std::max(g.nsm, 1);
+}
+void* pcgb::engine_swap_stream(void* s) {
+  if (!g.init) engine_init();
+  void* old = (void*)g.stream;
+  g.stream = (cudaStream_t)s;
+  return old;
+}
+
 extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (engine_init() || validate(p)) return nullptr;

@@ -1,15 +1,20 @@
 // server.cu -- request server with continuous batching over the box/batch API.
 //
-// A background thread runs rounds: it admits waiting requests in arrival
-// order while their device memory (pcgb_params_bytes) fits the budget and the
-// active count is below max_active, creates and seeds their boxes on the
-// device, advances every active box by `steps` RK3 steps (steps = the smaller
-// of round_steps and the fewest steps any active box still needs) with one
-// persistent batched launch per substep per class (precision, field count),
-// then retires finished boxes (diagnostics, optional copy of the final f),
-// which frees their memory for the next admissions.  Requests arriving while
-// a round runs join at the next round boundary.  max_active = 1 turns the
-// same loop into FIFO one-at-a-time service.
+// A background thread runs rounds.  Each round it admits waiting requests in
+// arrival order while their device memory (pcgb_params_bytes) fits the budget
+// and the active count is below max_active, creates and seeds their boxes on
+// the device, and picks the requests to advance: the oldest request and the
+// younger requests of its class (precision, field count, kernel variant) that
+// fit into the kernel waves the oldest one occupies on its own (tiles rounded
+// up to whole waves of the GPU), so batching never lengthens the oldest
+// request's substeps; when that leaves less than one wave of work on the
+// device, younger requests of the other classes fill it.  The picked requests
+// advance by `steps` RK3 steps (the smaller of round_steps and the fewest steps
+// any of them still needs) with one persistent batched launch per substep per
+// class, each class on its own stream so that the classes run side by side.
+// Finished boxes are retired (diagnostics, optional copy of the final f), which
+// frees their memory for the next admissions.  Requests arriving while a round
+// runs join at the next round.  max_active = 1 gives FIFO one-at-a-time service.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -20,8 +25,11 @@
 #include <thread>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "boundcond.h"
 #include "../../include/pcgb300.h"
+#include "params_check.h"
 #include "pcgb_box.h"
 
 namespace {
@@ -102,7 +110,23 @@ void pcgb_server::finish_box(Req* r, bool ok) {
   done_cv.notify_all();
 }
 
+static int class_key(const Req* r) {
+  const int upw = (r->p.lupw_uu || r->p.lupw_lnrho) ? 1 : 0;   // the upwinding kernel variant is its own class
+  return ((upw * 2 + r->p.dfloat) * 16 + r->p.precision) * 16 + (r->p.lentropy ? 8 : 7);
+}
+
+static long long box_tiles(pcgb_box* b) {
+  int v[8] = {0};
+  pcgb_box_info(b, v, 8);
+  return v[7];
+}
+
 void pcgb_server::run() {
+  // the server thread drives the engine: its own stream between rounds, one per class in them
+  cudaStream_t own = nullptr;
+  cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking);
+  void* prev_stream = pcgb::engine_swap_stream(own);
+  std::map<int, cudaStream_t> streams;
   while (true) {
     std::vector<Req*> admitted;
     {
@@ -142,20 +166,42 @@ void pcgb_server::run() {
     std::vector<Req*> act;
     {
       std::lock_guard<std::mutex> lk(mu);
-      act = active;
+      act = active;   // arrival order
     }
     if (act.empty()) continue;
+    // requests advanced this round: the oldest one, its class within the oldest one's waves,
+    // then (if less than one wave is busy) the other classes up to one wave
+    std::vector<Req*> sel;
+    {
+      Req* head = act[0];
+      const int hk = class_key(head);
+      const long long wave = pcgb::box_wave(head->box);
+      const long long cap = (box_tiles(head->box) + wave - 1) / wave * wave;
+      long long busy = 0;
+      std::vector<char> picked(act.size(), 0);
+      for (size_t i = 0; i < act.size(); ++i) {
+        const long long t = box_tiles(act[i]->box);
+        if (class_key(act[i]) == hk && (i == 0 || busy + t <= cap)) { sel.push_back(act[i]); busy += t; picked[i] = 1; }
+      }
+      if (busy < wave)
+        for (size_t i = 0; i < act.size(); ++i) {
+          const long long t = box_tiles(act[i]->box);
+          if (!picked[i] && busy + t <= wave) { sel.push_back(act[i]); busy += t; }
+        }
+    }
     int steps = round_steps;
-    for (Req* r : act) steps = std::min(steps, r->nsteps - r->done_steps);
+    for (Req* r : sel) steps = std::min(steps, r->nsteps - r->done_steps);
     if (steps < 1) steps = 1;
     // one batch per class; rebuilt when its membership changed
     std::map<int, std::vector<pcgb_box*>> cls;
-    for (Req* r : act) {
-      const int upw = (r->p.lupw_uu || r->p.lupw_lnrho) ? 1 : 0;   // the upwinding kernel variant is its own class
-      cls[((upw * 2 + r->p.dfloat) * 16 + r->p.precision) * 16 + (r->p.lentropy ? 8 : 7)].push_back(r->box);
-    }
+    for (Req* r : sel) cls[class_key(r)].push_back(r->box);
     bool ok = true;
+    std::vector<cudaStream_t> used_streams;
     for (auto& kv : cls) {
+      cudaStream_t& cs = streams[kv.first];
+      if (!cs) cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+      pcgb::engine_swap_stream(cs);
+      used_streams.push_back(cs);
       ClassBatch& cb = batches[kv.first];
       if (cb.members != kv.second || !cb.batch) {
         if (cb.batch) pcgb_batch_destroy(cb.batch);
@@ -165,6 +211,9 @@ void pcgb_server::run() {
       }
       if (pcgb_batch_steps(cb.batch, steps, 0, 0)) ok = false;
     }
+    for (cudaStream_t cs : used_streams)
+      if (cudaStreamSynchronize(cs) != cudaSuccess) ok = false;
+    pcgb::engine_swap_stream(own);
     for (auto it = batches.begin(); it != batches.end();) {
       if (!cls.count(it->first)) {
         if (it->second.batch) pcgb_batch_destroy(it->second.batch);
@@ -173,9 +222,9 @@ void pcgb_server::run() {
         ++it;
       }
     }
-    if (!act.empty()) pcgb_box_sync(act[0]->box);
+    if (pcgb_box_sync(sel[0]->box)) ok = false;
     ++rounds;
-    for (Req* r : act) {
+    for (Req* r : sel) {
       r->done_steps += steps;
       if (r->done_steps >= r->nsteps || !ok) {
         // the batch that holds this box is rebuilt next round (membership changes)
@@ -196,6 +245,11 @@ void pcgb_server::run() {
   for (auto& kv : batches)
     if (kv.second.batch) pcgb_batch_destroy(kv.second.batch);
   batches.clear();
+  cudaStreamSynchronize(own);
+  pcgb::engine_swap_stream(prev_stream);
+  for (auto& kv : streams)
+    if (kv.second) cudaStreamDestroy(kv.second);
+  cudaStreamDestroy(own);
 }
 
 extern "C" pcgb_server* pcgb_server_create(size_t mem_budget_bytes, int max_active, int round_steps) {

@@ -62,11 +62,42 @@ def run_plain(boxes, steps: int):
     boxes[0].sync()
 
 
-def autotune_batch(specs, tiles=(4, 5, 6, 7), zdepths=(16, 32, 64), steps: int = 3, sample: int = 24):
-    """Pick the tile variant and z-sweep depth for batched launches of this ensemble by
-    timing a sample of its boxes (every size present) in persistent launches.
-    Returns (tile, zdepth, table of ms per step)."""
+def _time_batch(specs, tile, zd_of, steps):
+    """ms per RK3 step of the given boxes in one persistent batched launch per substep."""
     import torch
+    boxes = []
+    for p, seed in specs:
+        q = default_params()
+        q.update(**p.as_dict())
+        q.tile, q.zdepth = tile, zd_of(q.nx)
+        b = Box(q)
+        init_box(b, q, seed)
+        boxes.append(b)
+    batch = Batch(boxes, persistent=True)
+    batch.steps(1, use_graph=False)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.ExternalStream(load().pcgb_get_stream())
+    t0.record(stream)
+    batch.steps(steps, use_graph=False)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    batch.close()
+    for b in boxes:
+        b.close()
+    return t0.elapsed_time(t1) / steps
+
+
+def autotune_batch(specs, tiles=(4, 5, 6, 7), zdepths=(16, 32, 64), steps: int = 3, sample: int = 24,
+                   per_size_zdepths=(8, 16, 32, 64, 128), per_size_sample: int = 6):
+    """Pick the tile variant of the batched launch and the z-sweep depth of every box size.
+
+    Stage 1 times the tile variants (with one z-depth for all boxes) on a sample of the
+    ensemble that holds every size; stage 2 keeps the best tile and times, size by size,
+    batches of that size's boxes at each z-depth up to the box height.  A launch carries
+    one tile shape (the kernel is compiled per shape); z-depths are per box.
+    Returns (tile, {size: zdepth}, table of ms per step)."""
     by_size = {}
     for p, seed in specs:
         by_size.setdefault(p.nx, []).append((p, seed))
@@ -81,37 +112,26 @@ def autotune_batch(specs, tiles=(4, 5, 6, 7), zdepths=(16, 32, 64), steps: int =
     table = {}
     for tile in tiles:
         for zd in zdepths:
-            boxes = []
-            for p, seed in pick:
-                q = default_params()
-                q.update(**p.as_dict())
-                q.tile, q.zdepth = tile, zd
-                b = Box(q)
-                init_box(b, q, seed)
-                boxes.append(b)
-            batch = Batch(boxes, persistent=True)
-            batch.steps(1, use_graph=False)
-            torch.cuda.synchronize()
-            t0 = torch.cuda.Event(enable_timing=True)
-            t1 = torch.cuda.Event(enable_timing=True)
-            stream = torch.cuda.ExternalStream(load().pcgb_get_stream())
-            t0.record(stream)
-            batch.steps(steps, use_graph=False)
-            t1.record(stream)
-            torch.cuda.synchronize()
-            table[(tile, zd)] = t0.elapsed_time(t1) / steps
-            batch.close()
-            for b in boxes:
-                b.close()
-    best = min(table, key=table.get)
-    return best[0], best[1], table
+            table[(tile, zd)] = _time_batch(pick, tile, lambda n, zd=zd: zd, steps)
+    best_tile, best_zd = min(table, key=table.get)
+    zd_by_size = {}
+    for n, lst in sorted(by_size.items()):
+        group = lst[:per_size_sample]
+        cands = [z for z in per_size_zdepths if z <= n] or [n]
+        times = {z: _time_batch(group, best_tile, lambda m, z=z: z, steps) for z in cands}
+        for z, ms in times.items():
+            table[(best_tile, f"{n}^3 zd {z}")] = ms
+        zd_by_size[n] = min(times, key=times.get)
+    return best_tile, zd_by_size, table
 
 
-def with_tiling(specs, tile: int, zdepth: int):
+def with_tiling(specs, tile: int, zdepth):
+    """Copies of specs with the tile variant and the z-depth (an int, or {size: zdepth})."""
     out = []
     for p, seed in specs:
         q = default_params()
         q.update(**p.as_dict())
-        q.tile, q.zdepth = tile, zdepth
+        q.tile = tile
+        q.zdepth = zdepth.get(q.nx, 0) if isinstance(zdepth, dict) else zdepth
         out.append((q, seed))
     return out
