@@ -60,3 +60,40 @@ def test_batch_cfl_per_box(pc, ic):
         res.append([(b.store(), b.time()) for b in boxes])
     for (fa, ta), (fb, tb) in zip(*res):
         assert np.array_equal(fa, fb) and ta == tb
+
+
+def test_tensor_memory_tile_batch_with_zdepth_per_box(pc, ic):
+    """FP32 pair tile 5 (z data in tensor memory) in one persistent launch over boxes of
+    uneven sizes, each with its own z-sweep depth and a ragged tiling (a CTA primes the
+    tensor-memory ring at the start of every tile it pulls): bitwise the same as each box
+    stepped alone with its default depth, with lagged CFL dt and diagnostics."""
+    shapes = [(32, 32, 32, 16), (48, 40, 24, 8), (37, 19, 11, 0), (64, 16, 40, 40), (24, 24, 24, 24)]
+
+    def mk(i, n, zd):
+        p = pc.default_params(nx=n[0], ny=n[1], nz=n[2], gamma=1.0, nu=2e-3 * (i + 1), eta=3e-3, dt=0.0,
+                              dt_mode=1, cdt=0.4, precision=4, comp=1, lforcing_cont=1, ampl_ff=0.02, kf=1.0 + i % 2,
+                              diag_every=2, tile=5, zdepth=zd)
+        f = ic.zeros(p)
+        ic.gaussian_noise(f, p, ["ux", "uy", "uz", "ax", "ay", "az"], 1e-2, 50 + i)
+        return p, f
+
+    singles = []
+    for i, s in enumerate(shapes):
+        p, f = mk(i, s[:3], 0)
+        b = pc.Box(p)
+        b.load(f)
+        b.steps(6)
+        singles.append((b.store(), b.time(), b.diag_raw()))
+        b.close()
+    boxes = []
+    for i, s in enumerate(shapes):
+        p, f = mk(i, s[:3], s[3])
+        b = pc.Box(p)
+        b.load(f)
+        boxes.append(b)
+    batch = pc.Batch(boxes, persistent=True)
+    batch.steps(6, use_graph=True, graph_steps=2)
+    for b, (fs, ts, ds) in zip(boxes, singles):
+        assert np.array_equal(b.store(), fs)
+        assert b.time() == ts
+        assert np.array_equal(b.diag_raw(), ds)

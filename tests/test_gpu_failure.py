@@ -52,3 +52,25 @@ def test_nan_in_host_state_is_flagged(pc, ic):
     with pytest.raises(pc.PcgbError, match="non-finite"):
         b.sync()
     L.pcgb_clear_error()
+
+
+def test_bounded_wait_timeout_tensor_memory_tile(pc, ic):
+    """The same timeout path in the FP32 pair kernel that holds tensor memory: the CTAs
+    leave their tiles, release their tensor memory and return; the next launches allocate
+    it again and the box steps normally after a reload."""
+    L = pc.load()
+    b, f = _box(pc, ic, precision=4, comp=1, tile=5)
+    try:
+        L.pcgb_set_wait_limit(2000)
+        L.pcgb_inject_wait_failure(1)
+        b.steps(1)
+        with pytest.raises(pc.PcgbError, match="bounded device wait"):
+            b.sync()
+    finally:
+        L.pcgb_inject_wait_failure(0)
+        L.pcgb_set_wait_limit(0)
+        L.pcgb_clear_error()
+    b.load(f)
+    b.steps(2)
+    b.sync()
+    assert np.all(np.isfinite(b.store()))
