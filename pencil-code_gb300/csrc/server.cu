@@ -195,24 +195,28 @@ void pcgb_server::run() {
     // one batch per class; rebuilt when its membership changed
     std::map<int, std::vector<pcgb_box*>> cls;
     for (Req* r : sel) cls[class_key(r)].push_back(r->box);
-    bool ok = true;
+    // a class whose launches could not be issued fails its members; otherwise every
+    // request's own device state decides (one box turning non-finite fails that box only)
+    std::map<int, bool> class_ok;
     std::vector<cudaStream_t> used_streams;
     for (auto& kv : cls) {
       cudaStream_t& cs = streams[kv.first];
       if (!cs) cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
       pcgb::engine_swap_stream(cs);
       used_streams.push_back(cs);
+      class_ok[kv.first] = true;
       ClassBatch& cb = batches[kv.first];
       if (cb.members != kv.second || !cb.batch) {
         if (cb.batch) pcgb_batch_destroy(cb.batch);
         cb.members = kv.second;
         cb.batch = pcgb_batch_create(cb.members.data(), (int)cb.members.size(), 1);
-        if (!cb.batch) { ok = false; continue; }
+        if (!cb.batch) { class_ok[kv.first] = false; continue; }
       }
-      if (pcgb_batch_steps(cb.batch, steps, 0, 0)) ok = false;
+      if (pcgb_batch_steps(cb.batch, steps, 0, 0)) class_ok[kv.first] = false;
     }
+    bool streams_ok = true;
     for (cudaStream_t cs : used_streams)
-      if (cudaStreamSynchronize(cs) != cudaSuccess) ok = false;
+      if (cudaStreamSynchronize(cs) != cudaSuccess) streams_ok = false;
     pcgb::engine_swap_stream(own);
     for (auto it = batches.begin(); it != batches.end();) {
       if (!cls.count(it->first)) {
@@ -222,9 +226,10 @@ void pcgb_server::run() {
         ++it;
       }
     }
-    if (pcgb_box_sync(sel[0]->box)) ok = false;
     ++rounds;
     for (Req* r : sel) {
+      const bool ok = streams_ok && class_ok[class_key(r)] && pcgb_box_sync(r->box) == 0;
+      if (!ok) pcgb_clear_error();
       r->done_steps += steps;
       if (r->done_steps >= r->nsteps || !ok) {
         // the batch that holds this box is rebuilt next round (membership changes)

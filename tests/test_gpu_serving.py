@@ -101,3 +101,27 @@ def test_upwinding_requests_in_the_mix(pc):
     for (n, prec, ent, seed, nu, k, steps, upw), f in zip(specs, outs):
         ref = _alone(pc, ens, req(n, prec, ent, seed, nu, k, upw), steps, seed)
         assert np.array_equal(f, ref), (n, prec, ent, upw)
+
+
+def test_failing_request_fails_alone(pc):
+    """A request whose state turns non-finite (initial noise of infinite amplitude) fails on
+    its own: the requests batched with it in the same class and rounds complete with the
+    results they give alone."""
+    serve = importlib.import_module("pencil-code_gb300.serve")
+    ens = importlib.import_module("pencil-code_gb300.ensemble")
+    specs = [(32, 4, False, 21, 2e-3, 1.0, 9), (32, 4, False, 22, 3e-3, 2.0, 9), (24, 4, False, 23, 4e-3, 1.0, 9)]
+    srv = serve.Server(budget_bytes=20e9, round_steps=3)
+    outs, ids = [], []
+    for i, (n, prec, ent, seed, nu, k, steps) in enumerate(specs):
+        p = _req(pc, n, prec, ent, seed, nu, k)
+        f = np.zeros(pc.host_shape(p), order="F")
+        outs.append(f)
+        ids.append(srv.submit(p, steps, seed, noise=float("inf") if i == 1 else 1e-5, f_out=f))
+    assert srv.drain(600)
+    rcs = [srv.poll(rid)[0] for rid in ids]
+    srv.close()
+    assert rcs == [1, -1, 1], rcs
+    for i in (0, 2):
+        n, prec, ent, seed, nu, k, steps = specs[i]
+        ref = _alone(pc, ens, _req(pc, n, prec, ent, seed, nu, k), steps, seed)
+        assert np.array_equal(outs[i], ref)
