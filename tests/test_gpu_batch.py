@@ -101,4 +101,6 @@ def test_tensor_memory_tile_batch_with_zdepth_per_box(pc, ic):
         assert np.array_equal(g, fs) and np.array_equal(g, fd)
         assert b.time() == ts == td
         assert np.array_equal(b.diag_raw(), ds)
-        assert np.allclose(ds, dd, rtol=1e-12, atol=0.0)
+        keep = np.arange(ds.size) != 7          # slot 7: sum of (div B)^2, pure round-off
+        assert np.allclose(ds[keep], dd[keep], rtol=1e-12, atol=0.0)
+        assert dd[7] <= 1e-10 * dd[8]
