@@ -68,7 +68,12 @@ typedef struct pcgb_params {
   double dt;               /* fixed dt; 0 selects the CFL timestep (ldt) */
   int dt_mode;             /* with dt == 0: 1 = lagged (reference GPU default), 2 = current (CPU semantics) */
   int diag_every;          /* device diagnostics every diag_every steps (0: on request only) */
-  int tile;                /* kernel tile variant, -1 = choose automatically */
+  int tile;                /* kernel tile variant, -1 = choose automatically.  FP32: 0-3 field-major
+                              (32,4) (32,8) (16,8) (64,4); 4-7 packed pairs (32,4) (32,8) (16,8)
+                              (32,12), 5 and 7 with the z data in tensor memory; FP64: (32,4)
+                              (16,8) (24,8) (32,6); double-float pairs 4-7: (24,8) (16,12) (16,8)
+                              (32,4).  Upwinding variants: FP32 tiles 1, 5, 6; FP64 1-3;
+                              double-float 2, 3, 5, 6. */
   int zdepth;              /* z-sweep depth, 0 = choose automatically */
   int dfloat;              /* precision 8 only: 1 = FP64-class state and arithmetic as double-float
                               pairs (hi + lo FP32, 48-bit significand) on the FP32 pipes instead of

@@ -1,21 +1,33 @@
 // cell_pair_tmem.cuh -- FP32 packed-pair cell policy whose z-direction data lives
 // in tensor memory (TMEM) instead of the shared-memory plane ring.
 //
-// Each thread owns one TMEM lane (its column of the tile) and a ring of 8
-// plane slots of 32 columns there.  When a plane arrives at the leading edge
-// of the stencil (plane z+3 of output plane z), the thread reads its centre
-// values and the x / y differences A_d = f(+d) - f(-d) (d = 1..3) that the
-// xz / yz mixed derivatives need from shared memory once, and stores them in
-// the plane's slot.  Output plane z then takes its z-stencils (der, der2) from
-// the centre values of planes z-3..z+3 and the bidiagonal xz / yz derivatives
+// Each thread owns one TMEM lane (its column of the tile).  When a plane
+// arrives at the leading edge of the stencil (plane z+3 of output plane z),
+// the thread reads its centre values and the x / y differences
+// A_d = f(+d) - f(-d) (d = 1..3) that the xz / yz mixed derivatives need from
+// shared memory once, and keeps them in tensor memory.  Output plane z then
+// takes its z-stencils (der, der2) from the centre values of planes z-3..z+3
+// and the bidiagonal xz / yz derivatives
 //   derij = fac (270 t1 - 27 t2 + 2 t3),  t_d = A_d(z+d) - A_d(z-d)
-// (deriv.f90:1387-1447) from the slots, with plane z's x / y stencils and the
-// xy derivative from shared memory as before.  Shared-memory loads per cell
-// drop from 149 to 107 (100 plus the six leading planes each tile primes) and
-// shared-memory wavefronts from 9.6 to 6.9 per cell; tensor memory has its own
-// data path.  The tcgen05 loads and stores are warp-collective, so the driver
-// runs step() on every lane of a warp that has a live cell (kWholeWarp) and the
-// cell masks its global accesses and reductions with `active`.
+// (deriv.f90:1387-1447) from there, with plane z's x / y stencils and the xy
+// derivative from shared memory as before.  Shared-memory loads per cell drop
+// from 149 to 107 and shared-memory wavefronts from 9.6 to 6.9 per cell;
+// tensor memory has its own data path.  The tcgen05 loads and stores are
+// warp-collective, so the driver runs step() on every lane of a warp that has
+// a live cell (kWholeWarp) and the cell masks its global accesses and
+// reductions with `active`.
+//
+// Two layouts, by the warps of the CTA (the SM's 512 columns are shared by
+// the warps w, w+4, w+8 of a lane quarter):
+//  * full (up to 8 warps, 256 columns a thread): a ring of 8 plane slots of 32
+//    columns, [0,8) centres, [8,16) A_1, [16,24) A_2, [24,32) A_3;
+//  * compact (12 warps, 160 columns a thread): centres in a ring of 8 slots
+//    [0,64), A_1 in a ring of 4 [64,96), A_2 in a ring of 8 [96,160); A_3 of
+//    plane z-3 is taken from the shared-memory ring (8 more shared loads).  The
+//    A_1 slot of plane z+3 is the one plane z-1 used, so it is written only
+//    after this step's loads have completed.
+// With 12 warps (168 registers) the SM issues from three warps per scheduler
+// instead of two.
 #pragma once
 
 #include "cell_pair.cuh"
@@ -56,38 +68,51 @@ struct PairCellTM {
   static constexpr int ILNRHO = 3, ISS = 4, IAX = NF - 3;
   static constexpr bool ENTROPY = (NF == 8);
   static constexpr int NWARP = (TX * TY + 31) / 32;
-  static constexpr int kColsPerThread = 256;                        // 8 plane slots x 32 columns
-  static constexpr int kTmemCols = kColsPerThread * ((NWARP + 3) / 4);   // warps w, w+4 share a lane quarter
-  static_assert(kTmemCols <= 512, "tensor memory holds 512 columns");
-  // slot layout: [0,8) centres (P0..P3), [8,16) A1, [16,24) A2, [24,32) A3, each A group
-  // (A^x of P0, A^x of P2, A^y of P1, A^y of P2) as float2
+  // each A group is (A^x of P0, A^x of P2, A^y of P1, A^y of P2) as float2
+  static constexpr bool kCompact = NWARP > 8;
+  static constexpr int kColsPerThread = kCompact ? 160 : 256;
+  static constexpr int kGroups = (NWARP + 3) / 4;                  // warps sharing a lane quarter
+  static_assert(kColsPerThread * kGroups <= 512, "tensor memory holds 512 columns");
+  static constexpr int kTmemCols = (kColsPerThread * kGroups <= 256) ? 256 : 512;   // a power of two
   static constexpr bool kWholeWarp = true;   // the driver calls step() for every lane of a live warp
 
   struct Tile : Base::Tile {
     uint32_t tm;   // this warp's lane quarter and column base
     int zfirst;
 
+    // TMEM address of plane zz's centres (part 0) or A_part differences
     __device__ __forceinline__ uint32_t slot(int zz, int part) const {
-      return tm + (uint32_t)(((zz & 7) << 5) + (part << 3));
+      if constexpr (kCompact)
+        return tm + (uint32_t)(part == 0 ? ((zz & 7) << 3) : (part == 1 ? 64 + ((zz & 3) << 3) : 96 + ((zz & 7) << 3)));
+      else
+        return tm + (uint32_t)(((zz & 7) << 5) + (part << 3));
     }
-    // leading plane zz of the stencil: centres and the A differences into TMEM;
-    // returns them for the caller's use on this step
-    __device__ __forceinline__ void lead(const float2* q, int zz, float2 cen[4], float2 a3[4]) {
-      const int o0 = 0, o1 = FO, o2 = 2 * FO, o3 = 3 * FO;
-      cen[0] = q[o0]; cen[1] = q[o1]; cen[2] = q[o2]; cen[3] = q[o3];
-      {
-        const float v[8] = {cen[0].x, cen[0].y, cen[1].x, cen[1].y, cen[2].x, cen[2].y, cen[3].x, cen[3].y};
-        tm_st8(slot(zz, 0), v);
-      }
+    // leading plane of the stencil: centres and the x / y differences A_1..A_3 from shared memory
+    __device__ __forceinline__ static void lead_read(const float2* q, float2 cen[4], float2 a[3][4]) {
+      cen[0] = q[0]; cen[1] = q[FO]; cen[2] = q[2 * FO]; cen[3] = q[3 * FO];
 #pragma unroll
       for (int d = 1; d <= 3; ++d) {
-        const float2 ax0 = p_sub(q[o0 + d], q[o0 - d]);
-        const float2 ax2 = p_sub(q[o2 + d], q[o2 - d]);
-        const float2 ay1 = p_sub(q[o1 + d * BW], q[o1 - d * BW]);
-        const float2 ay2 = p_sub(q[o2 + d * BW], q[o2 - d * BW]);
-        const float v[8] = {ax0.x, ax0.y, ax2.x, ax2.y, ay1.x, ay1.y, ay2.x, ay2.y};
-        tm_st8(slot(zz, d), v);
-        if (d == 3) { a3[0] = ax0; a3[1] = ax2; a3[2] = ay1; a3[3] = ay2; }
+        a[d - 1][0] = p_sub(q[d], q[-d]);
+        a[d - 1][1] = p_sub(q[2 * FO + d], q[2 * FO - d]);
+        a[d - 1][2] = p_sub(q[FO + d * BW], q[FO - d * BW]);
+        a[d - 1][3] = p_sub(q[2 * FO + d * BW], q[2 * FO - d * BW]);
+      }
+    }
+    __device__ __forceinline__ static void put8(uint32_t taddr, const float2 v[4]) {
+      const float w[8] = {v[0].x, v[0].y, v[1].x, v[1].y, v[2].x, v[2].y, v[3].x, v[3].y};
+      tm_st8(taddr, w);
+    }
+    // full layout: the leading plane zz's centres and A differences into its slot as they are
+    // formed; returns the centres and A_3 for the caller's use on this step
+    __device__ __forceinline__ void lead_full(const float2* q, int zz, float2 cen[4], float2 a3[4]) const {
+      cen[0] = q[0]; cen[1] = q[FO]; cen[2] = q[2 * FO]; cen[3] = q[3 * FO];
+      put8(slot(zz, 0), cen);
+#pragma unroll
+      for (int d = 1; d <= 3; ++d) {
+        const float2 a[4] = {p_sub(q[d], q[-d]), p_sub(q[2 * FO + d], q[2 * FO - d]),
+                             p_sub(q[FO + d * BW], q[FO - d * BW]), p_sub(q[2 * FO + d * BW], q[2 * FO - d * BW])};
+        put8(slot(zz, d), a);
+        if (d == 3) { a3[0] = a[0]; a3[1] = a[1]; a3[2] = a[2]; a3[3] = a[3]; }
       }
     }
 
@@ -98,21 +123,47 @@ struct PairCellTM {
       const Fac<float>& F = this->F;
       const Phys<float>& P = this->P;
       const long long cidx = (long long)(z + 3) * this->ps + (long long)(y + 3) * this->px + this->xoff + x;
-      if (z == zfirst) {   // prologue of the tile: planes z-3..z+2 into their slots
-        float2 c_[4], a_[4];
+      float2 cL[4], aL[3][4];   // the leading plane z+3 (aL[0], aL[1]: compact layout only)
+      if constexpr (!kCompact) {
+        if (z == zfirst) {   // prologue of the tile: planes z-3..z+2 into their slots
+          float2 c_[4], a_[4];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) this->lead(pl[k], z - 3 + k, c_, a_);
+          for (int k = 0; k < 6; ++k) lead_full(pl[k], z - 3 + k, c_, a_);
+        }
+        tm_wait_st();   // earlier slots are written before they are read below
+        lead_full(pl[6], z + 3, cL, aL[2]);
+      } else {
+        if (z == zfirst) {   // prologue: planes z-3..z+2, only the slots read later
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            float2 c_[4], a_[3][4];
+            lead_read(pl[k], c_, a_);
+            put8(slot(z - 3 + k, 0), c_);
+            if (k >= 2) put8(slot(z - 3 + k, 1), a_[0]);
+            if (k >= 1) put8(slot(z - 3 + k, 2), a_[1]);
+          }
+        }
+        tm_wait_st();
+        lead_read(pl[6], cL, aL);
+        put8(slot(z + 3, 0), cL);   // slots that no load of this step reads
+        put8(slot(z + 3, 2), aL[1]);
       }
-      tm_wait_st();   // earlier slots are written before they are read below
-      float2 cL[4], a3L[4];
-      lead(pl[6], z + 3, cL, a3L);
       // xz / yz mixed derivatives from the A slots of planes z+-1, z+-2, z-3 (and z+3 in registers)
       uint32_t ra1p[8], ra1m[8], ra2p[8], ra2m[8], ra3m[8];
       tm_ld8(slot(z + 1, 1), ra1p);
       tm_ld8(slot(z - 1, 1), ra1m);
       tm_ld8(slot(z + 2, 2), ra2p);
       tm_ld8(slot(z - 2, 2), ra2m);
-      tm_ld8(slot(z - 3, 3), ra3m);
+      float2 a3m[4];   // A_3 of plane z-3
+      if constexpr (!kCompact) {
+        tm_ld8(slot(z - 3, 3), ra3m);
+      } else {
+        const float2* q = pl[0];
+        a3m[0] = p_sub(q[3], q[-3]);
+        a3m[1] = p_sub(q[2 * FO + 3], q[2 * FO - 3]);
+        a3m[2] = p_sub(q[FO + 3 * BW], q[FO - 3 * BW]);
+        a3m[3] = p_sub(q[2 * FO + 3 * BW], q[2 * FO - 3 * BW]);
+      }
       float2 dfo2[4];
 #pragma unroll
       for (int p = 0; p < 4; ++p) dfo2[p] = this->dfnext[p];
@@ -125,13 +176,20 @@ struct PairCellTM {
         for (int p = 0; p < 4; ++p) prefetch_l2(this->dfp + p * this->fs + cidx + kDfPrefetch * this->ps);
       }
       tm_wait_ld();
-      tm_tie8(ra1p); tm_tie8(ra1m); tm_tie8(ra2p); tm_tie8(ra2m); tm_tie8(ra3m);
+      tm_tie8(ra1p); tm_tie8(ra1m); tm_tie8(ra2p); tm_tie8(ra2m);
+      if constexpr (!kCompact) {
+        tm_tie8(ra3m);
+#pragma unroll
+        for (int g = 0; g < 4; ++g) a3m[g] = u2f2(ra3m[2 * g], ra3m[2 * g + 1]);
+      } else {
+        put8(slot(z + 3, 1), aL[0]);   // the A_1 slot just read for plane z-1
+      }
       float2 mz[4];   // (u_x,xz A_1,xz) (u_z,xz A_3,xz) (u_y,yz A_2,yz) (u_z,yz A_3,yz)
 #pragma unroll
       for (int g = 0; g < 4; ++g) {
         const float2 t1 = p_sub(u2f2(ra1p[2 * g], ra1p[2 * g + 1]), u2f2(ra1m[2 * g], ra1m[2 * g + 1]));
         const float2 t2 = p_sub(u2f2(ra2p[2 * g], ra2p[2 * g + 1]), u2f2(ra2m[2 * g], ra2m[2 * g + 1]));
-        const float2 t3 = p_sub(a3L[g], u2f2(ra3m[2 * g], ra3m[2 * g + 1]));
+        const float2 t3 = p_sub(aL[2][g], a3m[g]);
         const float fac = (g < 2) ? F.mxz : F.myz;
         const float2 r = p_fma(p_splat(2.f), t3, p_fma(p_splat(-27.f), t2, p_mul(p_splat(270.f), t1)));
         mz[g] = p_mul(p_splat(fac), r);

@@ -12,9 +12,10 @@ namespace pcgb {
 // Tile variants.  Ids 0..3 use the field-major layout (one value per field per
 // cell); for FP32 and double-float, ids 4..7 use the packed field-pair layout
 // (cell_pair.cuh: float2 elements; cell_ddpair.cuh: 16-byte dd2 elements).  The
-// default FP32 pair tile 5 keeps its z-direction data in tensor memory
-// (cell_pair_tmem.cuh); its upwinding variant is the shared-memory PairCell.
-//   FP32: 0 (32,4)x2  1 (32,8)  2 (16,8)x2  3 (64,4)  4 pair(32,4)x2  5 pair(32,8)  6 pair(16,8)x2  7 pair(64,4)
+// FP32 pair tiles 5 (8 warps) and 7 (12 warps, the default for large boxes)
+// keep their z-direction data in tensor memory (cell_pair_tmem.cuh); the
+// upwinding variant of tile 5 is the shared-memory PairCell, tile 7 has none.
+//   FP32: 0 (32,4)x2  1 (32,8)  2 (16,8)x2  3 (64,4)  4 pair(32,4)x2  5 pair(32,8)  6 pair(16,8)x2  7 pair(32,12)
 //   FP64: 0 (32,4)  1 (16,8)  2 (24,8)  3 (32,6)
 //   double-float: 0..3 as FP64, 4 pair(24,8)  5 pair(16,12)  6 pair(16,8)  7 pair(32,4)
 // (FP64-family rings of 8 planes fit one CTA per SM; the 192-thread tiles
@@ -29,12 +30,16 @@ inline int num_tiles(int dtype_bytes, int dfl = 0) {
 inline bool tile_is_pair(int dtype_bytes, int tile, int dfl = 0) {
   return (dtype_bytes == 4 || dfl) && tile >= kNumScalarTiles;
 }
+// Namespace-scope constexpr tables have internal linkage.  (Static locals of an
+// inline function would be one process-wide "unique" symbol, shared by every
+// library built from these sources that a process loads.)
+constexpr TileShape kF32Tiles[kNumScalarTiles] = {{32, 4}, {32, 8}, {16, 8}, {64, 4}};
+constexpr TileShape kF32PairTiles[kNumScalarTiles] = {{32, 4}, {32, 8}, {16, 8}, {32, 12}};
+constexpr TileShape kF64Tiles[kNumScalarTiles] = {{32, 4}, {16, 8}, {24, 8}, {32, 6}};
+constexpr TileShape kDdPairTiles[kNumScalarTiles] = {{24, 8}, {16, 12}, {16, 8}, {32, 4}};
 inline TileShape tile_shape(int dtype_bytes, int tile, int dfl = 0) {
-  static const TileShape f32[kNumScalarTiles] = {{32, 4}, {32, 8}, {16, 8}, {64, 4}};
-  static const TileShape f64[kNumScalarTiles] = {{32, 4}, {16, 8}, {24, 8}, {32, 6}};
-  static const TileShape ddp[kNumScalarTiles] = {{24, 8}, {16, 12}, {16, 8}, {32, 4}};
-  if (dtype_bytes == 4) return f32[tile % kNumScalarTiles];
-  return (dfl && tile >= kNumScalarTiles) ? ddp[tile - kNumScalarTiles] : f64[tile % kNumScalarTiles];
+  if (dtype_bytes == 4) return tile >= kNumScalarTiles ? kF32PairTiles[tile - kNumScalarTiles] : kF32Tiles[tile];
+  return (dfl && tile >= kNumScalarTiles) ? kDdPairTiles[tile - kNumScalarTiles] : kF64Tiles[tile % kNumScalarTiles];
 }
 
 struct KernelHandle {
@@ -125,7 +130,7 @@ static KernelHandle make_kernel_handle() {
           case 4: cache[4] = make_kernel_handle<PairCell<NF, 32, 4>, 32, 4, 8, 2>(); break;        \
           case 5: cache[5] = make_kernel_handle<PairCellTM<NF, 32, 8>, 32, 8, 9, 1>(); break;      \
           case 6: cache[6] = make_kernel_handle<PairCell<NF, 16, 8>, 16, 8, 8, 2>(); break;        \
-          default: cache[7] = make_kernel_handle<PairCell<NF, 64, 4>, 64, 4, 8, 1>(); break;       \
+          default: cache[7] = make_kernel_handle<PairCellTM<NF, 32, 12>, 32, 12, 9, 1>(); break;   \
         }                                                                                          \
       } else {                                                                                     \
         switch (tile) {                                                                            \

@@ -275,25 +275,43 @@ static int encode_maps(pcgb_box* b) {
 
 static int default_zdepth(const pcgb_box* b) {
   const int ntx = (b->nx + b->tx - 1) / b->tx, nty = (b->ny + b->ty - 1) / b->ty;
+  const long long cols = (long long)ntx * nty;
+  const long long wave = pcgb::box_wave(b);
+  if (cols >= 4 * wave) {
+    // enough column tiles for four waves: split z only where that evens out the
+    // last wave; cost = waves x (planes of a tile + 10 for the ring prologue and
+    // the tile's bookkeeping)
+    int best = b->nz;
+    long long best_cost = -1;
+    for (int k = 1; k <= 8; ++k) {
+      const int zd = (b->nz + k - 1) / k;
+      if (k > 1 && zd < 16) break;
+      const long long tiles = cols * ((b->nz + zd - 1) / zd);
+      const long long cost = ((tiles + wave - 1) / wave) * (zd + 10);
+      if (best_cost < 0 || cost < best_cost) { best_cost = cost; best = zd; }
+    }
+    return best;
+  }
   int zd = b->nz;
   // split z until there are enough tiles for ~4 waves of one CTA per SM
-  while (zd > 16 && (long long)ntx * nty * ((b->nz + zd - 1) / zd) < 4LL * g.nsm) zd = (zd + 1) / 2;
+  while (zd > 16 && cols * ((b->nz + zd - 1) / zd) < 4LL * g.nsm) zd = (zd + 1) / 2;
   return zd;
 }
 
-// FP32: packed pairs on (32,8) tiles, one 8-warp CTA per SM, when a box has
-// at least a wave of such column tiles, else on (16,8) tiles with two CTAs
-// per SM (more, smaller work items for small boxes); double-float: packed
+// FP32: packed pairs on (32,12) tiles, one 12-warp CTA per SM (on (32,8)
+// tiles, 8 warps, with upwinding or entropy), when a box has at least a wave
+// of (32,8) column tiles, else on (16,8) tiles with two CTAs per SM (more,
+// smaller work items for small boxes); double-float: packed
 // pairs on (16,12) tiles, one 6-warp CTA per SM; FP64: one 6-warp CTA per SM,
 // (32,6) with 7 fields, (24,8) with 8 (an 8-field ring of (32,6) planes needs
 // 246 KB of shared memory)
-static int default_tile(int tb, int nf, int dfl, int nx, int ny) {
-  if (tb == 4) return ((long long)((nx + 31) / 32) * ((ny + 7) / 8) >= 152) ? 5 : 6;
+static int default_tile(int tb, int nf, int dfl, int nx, int ny, bool upw) {
+  if (tb == 4) return ((long long)((nx + 31) / 32) * ((ny + 7) / 8) >= 152) ? ((upw || nf == 8) ? 5 : 7) : 6;
   return dfl ? 5 : (nf == 8 ? 2 : 3);
 }
 
 static int set_tiling(pcgb_box* b, int tile, int zd) {
-  if (tile < 0) tile = default_tile(b->tb, b->nf, b->dfl, b->nx, b->ny);
+  if (tile < 0) tile = default_tile(b->tb, b->nf, b->dfl, b->nx, b->ny, b->hdev.lupw != 0);
   if (tile >= num_tiles(b->tb, b->dfl)) return set_err(PCGB_E_ARG, "tile variant %d out of range", tile);
   if ((int)tile_is_pair(b->tb, tile, b->dfl) != b->pairs)
     return set_err(PCGB_E_ARG, "tile %d needs a different device layout than this box was created with", tile);
@@ -366,7 +384,7 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   b->nx = p->nx; b->ny = p->ny; b->nz = p->nz;
   b->mx = p->nx + 6; b->my = p->ny + 6; b->mz = p->nz + 6;
   {
-    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb, b->nf, b->dfl, p->nx, p->ny);
+    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb, b->nf, b->dfl, p->nx, p->ny, p->lupw_uu || p->lupw_lnrho);
     b->pairs = (t0 < num_tiles(b->tb, b->dfl) && tile_is_pair(b->tb, t0, b->dfl)) ? 1 : 0;
   }
   b->eb = b->pairs ? (b->dfl ? 16 : 8) : b->tb;
@@ -428,7 +446,7 @@ extern "C" size_t pcgb_params_bytes(const pcgb_params* p) {
   if (!p || p->nx < 1 || p->ny < 1 || p->nz < 1 || (p->precision != 4 && p->precision != 8)) return 0;
   const int tb = p->precision, nf = p->lentropy ? 8 : 7;
   const int dfl = (tb == 8 && p->dfloat) ? 1 : 0;
-  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb, nf, dfl, p->nx, p->ny);
+  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb, nf, dfl, p->nx, p->ny, p->lupw_uu || p->lupw_lnrho);
   const int pairs = (t0 < num_tiles(tb, dfl) && tile_is_pair(tb, t0, dfl)) ? 1 : 0;
   const int eb = pairs ? (dfl ? 16 : 8) : tb, ns = pairs ? 4 : nf;
   const int xoff = 128 / eb;
@@ -1141,7 +1159,11 @@ static int box_reload(pcgb_box* b, const pcgb_params& p) {
   fill_physics(b);
   int rc = upload_forcing(b);
   if (rc) return rc;
-  if ((b->hdev.lupw != 0) != (upw_was != 0) && (rc = set_tiling(b, b->tile, b->zd))) return rc;   // kernel variant
+  // kernel variant; a box on the default tile takes the default tile of its new physics
+  // (the default FP32 tile has no upwinding variant)
+  if ((b->hdev.lupw != 0) != (upw_was != 0) &&
+      (rc = p.tile >= 0 ? set_tiling(b, b->tile, b->zd) : set_tiling(b, -1, p.zdepth)))
+    return rc;
   CK(cudaMemcpyAsync(b->ddev, &b->hdev, sizeof(PcgbBoxDev), cudaMemcpyHostToDevice, g.stream));
   if (p.dt > 0) return pcgb_box_set_dt(b, p.dt);
   CK(cudaStreamSynchronize(g.stream));

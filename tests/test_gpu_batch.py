@@ -62,8 +62,9 @@ def test_batch_cfl_per_box(pc, ic):
         assert np.array_equal(fa, fb) and ta == tb
 
 
-def test_tensor_memory_tile_batch_with_zdepth_per_box(pc, ic):
-    """FP32 pair tile 5 (z data in tensor memory) in one persistent launch over boxes of
+@pytest.mark.parametrize("tile", [5, 7])
+def test_tensor_memory_tile_batch_with_zdepth_per_box(pc, ic, tile):
+    """FP32 pair tiles 5 and 7 (z data in tensor memory) in one persistent launch over boxes of
     uneven sizes, each with its own z-sweep depth and a ragged tiling (a CTA primes the
     tensor-memory ring at the start of every tile it pulls): bitwise the same as each box
     stepped alone with the same depth, with lagged CFL dt and diagnostics; the fields are
@@ -74,7 +75,7 @@ def test_tensor_memory_tile_batch_with_zdepth_per_box(pc, ic):
     def mk(i, n, zd):
         p = pc.default_params(nx=n[0], ny=n[1], nz=n[2], gamma=1.0, nu=2e-3 * (i + 1), eta=3e-3, dt=0.0,
                               dt_mode=1, cdt=0.4, precision=4, comp=1, lforcing_cont=1, ampl_ff=0.02, kf=1.0 + i % 2,
-                              diag_every=2, tile=5, zdepth=zd)
+                              diag_every=2, tile=tile, zdepth=zd)
         f = ic.zeros(p)
         ic.gaussian_noise(f, p, ["ux", "uy", "uz", "ax", "ay", "az"], 1e-2, 50 + i)
         return p, f

@@ -54,12 +54,13 @@ def test_nan_in_host_state_is_flagged(pc, ic):
     L.pcgb_clear_error()
 
 
-def test_bounded_wait_timeout_tensor_memory_tile(pc, ic):
-    """The same timeout path in the FP32 pair kernel that holds tensor memory: the CTAs
-    leave their tiles, release their tensor memory and return; the next launches allocate
-    it again and the box steps normally after a reload."""
+@pytest.mark.parametrize("tile", [5, 7])
+def test_bounded_wait_timeout_tensor_memory_tile(pc, ic, tile):
+    """The same timeout path in the FP32 pair kernels that hold tensor memory (8 and 12
+    warps): the CTAs leave their tiles, release their tensor memory and return; the next
+    launches allocate it again and the box steps normally after a reload."""
     L = pc.load()
-    b, f = _box(pc, ic, precision=4, comp=1, tile=5)
+    b, f = _box(pc, ic, precision=4, comp=1, tile=tile)
     try:
         L.pcgb_set_wait_limit(2000)
         L.pcgb_inject_wait_failure(1)

@@ -248,7 +248,7 @@ def test_isothermal_fp32_compensated(pc, ic, orc, tile):
     assert np.all(err <= TOL32), err
 
 
-@pytest.mark.parametrize("tile", [0, 4, 5])
+@pytest.mark.parametrize("tile", [0, 4, 5, 7])
 def test_entropy_fp32(pc, ic, orc, tile):
     p = pc.default_params(nx=32, ny=32, nz=32, lentropy=1, gamma=5.0 / 3.0, nu=2e-3, eta=2e-3, chi=2e-3,
                           dt=1e-3, precision=4, comp=1, tile=tile)
@@ -294,9 +294,9 @@ def test_tiles_cross_agree(pc, ic):
         assert np.all(rel_err(g, outs[0]) <= 1e-14)
 
 
-@pytest.mark.parametrize("tile", [4, 5])
+@pytest.mark.parametrize("tile", [4, 5, 7])
 def test_fp32_pair_layout_diagnostics_and_cfl(pc, ic, orc, tile):
-    """Packed-pair FP32 kernel (tile 5: z-direction data in tensor memory): diagnostics (FP64
+    """Packed-pair FP32 kernel (tiles 5 and 7: z-direction data in tensor memory, 8 and 12 warps): diagnostics (FP64
     sums of FP32 cell values) and the lagged CFL dt agree with the FP64 oracle to FP32 round-off."""
     p = iso_params(pc, precision=4, comp=1, tile=tile, dt=0.0, dt_mode=2, cdt=0.4, diag_every=1,
                    b_ext=(0.0, 0.1, 0.0), lforcing_cont=1, ampl_ff=0.05, kf=2.0)
