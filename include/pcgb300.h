@@ -380,7 +380,8 @@ int pcgb_substep_noalloc(const pcgb_params* p, int isubstep, double dt, const vo
                          double* reductions, void* stream);
 
 /* Iteration limit of every bounded wait on a TMA copy inside the substep
-   kernel (0 restores the default, about a second).  When a wait runs out the
+   kernel; one iteration is a suspended wait of at most 1 microsecond (0
+   restores the default, 2^21 iterations: about two seconds).  When a wait runs out the
    kernel records PCGB_ERR_TIMEOUT in the box state, waits for its own copies
    still in flight, and returns; the next pcgb_box_sync/store reports the
    error and the box must be reloaded.  Used by the failure-detection tests. */

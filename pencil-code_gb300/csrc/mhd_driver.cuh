@@ -32,7 +32,7 @@ namespace pcgb {
 
 // Bound of the wait for copies still in flight after a failed wait: long
 // enough for any TMA load to land, so a CTA never leaves with copies pending.
-constexpr unsigned int kDrainWaitLimit = 1u << 26;
+constexpr unsigned int kDrainWaitLimit = 1u << 22;
 
 // Cells that keep state in tensor memory declare kTmemCols (columns the CTA
 // allocates) and kColsPerThread; the others use none.

