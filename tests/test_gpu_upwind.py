@@ -137,6 +137,25 @@ def test_reload_switches_kernel_variant(pc, ic, orc):
     _check(f, ref, p1, "f64")
 
 
+def test_reload_switches_default_fp32_tile(pc, ic, orc):
+    """An FP32 box large enough for the default 12-warp tile (which has no upwinding variant),
+    created without upwinding: reloadConfig turning upwinding on moves it to the default tile
+    of the new physics, and the steps match the oracle."""
+    gpu = importlib.import_module("pencil-code_gb300.gpu")
+    n = (512, 80, 8)   # 16 x 10 column tiles of (32,8): the default FP32 tile is then tile 7
+    p0 = _params(pc, n=n, precision=4, comp=1, lupw_uu=0, lupw_lnrho=0)
+    f0 = 0.01 * _initial(pc, ic, p0, seed=12)   # grid noise of 5e-4, so that B = curl A stays O(0.1) at dx = 2 pi / 512
+    f = np.array(f0, order="F", copy=True)   # the REAL=double library; the device state is FP32
+    gpu.initialize_gpu(f, p0, t=0.0, nt=1)
+    p1 = _params(pc, n=n, precision=4, comp=1)
+    gpu.reload_gpu_config(p1)
+    gpu.time_step(3)
+    gpu.copy_farray_from_gpu(f)
+    gpu.finalize_gpu()
+    ref, _ = _oracle(orc, p1, f0, 3)
+    _check(f, ref, p1, "f32pair")
+
+
 def _timing_kvectors():
     """A small shell of the forcing wavevectors (|k|^2 in [5, 6]), ordered as k.dat lists them."""
     nl = importlib.import_module("pencil-code_gb300.namelist")
