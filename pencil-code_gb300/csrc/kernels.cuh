@@ -45,9 +45,14 @@ inline TileShape tile_shape(int dtype_bytes, int tile, int dfl = 0) {
 struct KernelHandle {
   const void* fn = nullptr;        // with CFL / diagnostic reductions
   const void* fn_nored = nullptr;  // without (same shared memory and block)
+  const void* fn_comp[3] = {nullptr, nullptr, nullptr};   // reduction-free, compensated, substep s (tiles 5, 7)
   int smem = 0;
   int threads = 0;
-  const void* pick(bool red) const { return red ? fn : fn_nored; }
+  // the kernel for a launch; s (0..2) and comp describe every box of the launch, s < 0 if they differ
+  const void* pick(bool red, int s = -1, bool comp = false) const {
+    if (!red && comp && s >= 0 && s < 3 && fn_comp[s]) return fn_comp[s];
+    return red ? fn : fn_nored;
+  }
 };
 
 // Defined in kernels_<type>_<nf>.cu.
@@ -87,7 +92,7 @@ inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile, int dfl = 0, b
   return nf == 8 ? kernel_f64_8(tile) : kernel_f64_7(tile);
 }
 
-template <class CELL, int TX, int TY, int R, int MB>
+template <class CELL, int TX, int TY, int R, int MB, bool SPEC = false>
 static KernelHandle make_kernel_handle();
 
 // Pair tiles of the double-float family (no kernel for the other element types).
@@ -97,7 +102,8 @@ static KernelHandle make_dd_pair_handle() {
   else return KernelHandle();
 }
 
-template <class CELL, int TX, int TY, int R, int MB>
+// SPEC: also the substep-specialised compensated variants (KIND 1..3)
+template <class CELL, int TX, int TY, int R, int MB, bool SPEC>
 static KernelHandle make_kernel_handle() {
   KernelHandle h;
   h.fn = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, true>);
@@ -108,6 +114,12 @@ static KernelHandle make_kernel_handle() {
                        h.smem);
   cudaFuncSetAttribute(&mhd_substep_kernel<CELL, TX, TY, R, MB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        h.smem);
+  if constexpr (SPEC) {
+    h.fn_comp[0] = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, false, 1>);
+    h.fn_comp[1] = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, false, 2>);
+    h.fn_comp[2] = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, false, 3>);
+    for (const void* fn : h.fn_comp) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, h.smem);
+  }
   return h;
 }
 
@@ -128,9 +140,9 @@ static KernelHandle make_kernel_handle() {
           case 2: cache[2] = make_kernel_handle<ScalarCell<T, NF, 16, 8>, 16, 8, 9, 2>(); break;   \
           case 3: cache[3] = make_kernel_handle<ScalarCell<T, NF, 64, 4>, 64, 4, 9, 1>(); break;   \
           case 4: cache[4] = make_kernel_handle<PairCell<NF, 32, 4>, 32, 4, 8, 2>(); break;        \
-          case 5: cache[5] = make_kernel_handle<PairCellTM<NF, 32, 8>, 32, 8, 9, 1>(); break;      \
+          case 5: cache[5] = make_kernel_handle<PairCellTM<NF, 32, 8>, 32, 8, 9, 1, true>(); break; \
           case 6: cache[6] = make_kernel_handle<PairCell<NF, 16, 8>, 16, 8, 8, 2>(); break;        \
-          default: cache[7] = make_kernel_handle<PairCellTM<NF, 32, 12>, 32, 12, 9, 1>(); break;   \
+          default: cache[7] = make_kernel_handle<PairCellTM<NF, 32, 12>, 32, 12, 9, 1, true>(); break; \
         }                                                                                          \
       } else {                                                                                     \
         switch (tile) {                                                                            \

@@ -57,7 +57,7 @@ struct DriverCfg {
   static constexpr int PLANE_BYTES = CELL::NSLICE * BW * BH * (int)sizeof(Elem);
   static constexpr int SLOT_BYTES = (PLANE_BYTES + 127) / 128 * 128;
   static constexpr int BAR_OFF = RING * SLOT_BYTES;                  // RING slot barriers + one never armed
-  static constexpr int CNT_OFF = BAR_OFF + (RING + 1) * 8;           // RING release counters, abort flag, issued
+  static constexpr int CNT_OFF = BAR_OFF + (RING + 1) * 8;           // RING release counters, a spare word, issued
   static constexpr int RED_OFF = CNT_OFF + ((RING + 2) * 4 + 7) / 8 * 8;
   static constexpr int SMEM_BYTES = RED_OFF + NWARP * PCGB_NSLOT * 8 + 64;
 };
@@ -66,15 +66,20 @@ struct DriverCfg {
 // and 3, and substep 1 with a fixed dt and no diagnostics due): no per-thread
 // FP64 accumulators, no reduction code.  The host picks it; a box that
 // nevertheless finds a reduction due flags PCGB_ERR_NORED.
-template <class CELL, int TX, int TY, int RING, int MINB, bool RED>
+// KIND = 1..3: reduction-free and specialised at compile time for substep
+// KIND-1 of boxes in the FP32 compensated mode, so that the substep's branches
+// of the update (df read and written, the carry's form) fold away; the host
+// picks it for such launches, a box in another substep or mode flags
+// PCGB_ERR_VARIANT.  KIND = 0: the substep and mode are read at run time.
+template <class CELL, int TX, int TY, int RING, int MINB, bool RED, int KIND = 0>
 __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs args) {
+  static_assert(KIND == 0 || !RED, "substep-specialised kernels are reduction-free");
   using C = DriverCfg<CELL, TX, TY, RING>;
   using T = typename CELL::T;
   using Elem = typename CELL::Elem;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::BAR_OFF);
   unsigned int* released = reinterpret_cast<unsigned int*>(smem + C::CNT_OFF);   // [RING]
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + C::CNT_OFF + RING * 4);
   unsigned int* issued = reinterpret_cast<unsigned int*>(smem + C::CNT_OFF + (RING + 1) * 4);
   double* red = reinterpret_cast<double*>(smem + C::RED_OFF);
   int* sh = reinterpret_cast<int*>(smem + C::RED_OFF + C::NWARP * PCGB_NSLOT * 8);
@@ -94,7 +99,6 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
   if (tid == 0) {
     for (int r = 0; r <= RING; ++r) mbar_init(&full[r], 1);   // full[RING]: never arrived on
     for (int r = 0; r < RING; ++r) released[r] = 0u;
-    *abort_flag = 0;
     fence_mbar_init();
   }
   if constexpr (TMC > 0) asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -143,7 +147,8 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
     const int nplanes = (z1 - z0) + 6;
 
     const unsigned long long nsub = __ldcg(&S->nsub);
-    const int s = (int)(nsub % 3ull);
+    const int s = KIND > 0 ? KIND - 1 : (int)(nsub % 3ull);
+    if (KIND > 0 && ((int)(nsub % 3ull) != s || B.comp == 0) && threadIdx.x == 0) atomicOr(&S->err, PCGB_ERR_VARIANT);
     const int inb = (int)(nsub & 1ull);
     const CUtensorMap* tmap = &B.tmap[inb];
     const double dt = __ldcg(&S->dt);
@@ -155,7 +160,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
                    ((B.diag_every > 0 && (step % (unsigned long long)B.diag_every) == 0ull) ||
                     __ldcg(&S->diag_request) != 0);
     fl.want_cfl = mode_cfl || (s == 0 && B.dt_mode == PCGB_DT_LAGGED);
-    fl.comp = (B.comp != 0);
+    fl.comp = KIND > 0 || B.comp != 0;
     fl.read_df = (s > 0) || fl.comp;
     fl.write_df = (s < 2) || fl.comp;
     fl.alpha = T(rk_alpha(s));
@@ -221,9 +226,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
       }
       // failure-detection test hook: a flag that nothing sets, waited for with the same bound
       if (args.inject_wait_failure && !mbar_wait_bounded(&full[RING], 0u, args.wait_limit)) lfail = 1;
-      // a failed wait in one warp stops every warp of the CTA
-      if (__any_sync(0xffffffffu, lfail)) *abort_flag = 1;
-      if (*abort_flag) {
+      // a warp whose wait failed leaves the tile; the others stop at their next wait, which
+      // then fails too (that warp no longer releases planes), and the CTA agrees below
+      if (__any_sync(0xffffffffu, lfail)) {
         failed = 1;
         break;
       }

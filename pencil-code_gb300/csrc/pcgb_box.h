@@ -88,3 +88,4 @@ struct alignas(64) PcgbBoxState {
 #define PCGB_ERR_TIMEOUT 2     // a bounded wait gave up
 #define PCGB_ERR_DT 4          // dt <= 0 or not finite
 #define PCGB_ERR_NORED 8       // a CFL or diagnostic reduction was due in a launch of the reduction-free kernel
+#define PCGB_ERR_VARIANT 16    // a kernel specialised for another substep or state mode was launched for the box

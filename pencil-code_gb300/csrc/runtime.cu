@@ -473,9 +473,10 @@ extern "C" int pcgb_box_info(const pcgb_box* b, int* info, int ninfo) {
 
 static int cur_in(const pcgb_box* b) { return (int)(b->nsub & 1ull); }
 
-// Launch one substep (or CFL pass) over boxes[0..n) of one class.
+// Launch one substep (or CFL pass) over boxes[0..n) of one class; s (0..2, or -1 when
+// the boxes differ) and comp (every box compensated FP32) select a specialised kernel.
 static int launch(const PcgbBoxDev* dboxes, int nboxes, int total_tiles, unsigned int* counter, int mode,
-                  const KernelHandle& kh, int grid, bool red) {
+                  const KernelHandle& kh, int grid, bool red, int s = -1, bool comp = false) {
   LaunchArgs a;
   a.boxes = dboxes;
   a.nboxes = nboxes;
@@ -486,7 +487,7 @@ static int launch(const PcgbBoxDev* dboxes, int nboxes, int total_tiles, unsigne
   a.inject_wait_failure = g.inject_wait_failure;
   if (counter) CK(cudaMemsetAsync(counter, 0, sizeof(unsigned int), g.stream));
   void* args[] = {&a};
-  CK(cudaLaunchKernel(kh.pick(red || mode == MODE_CFL), dim3(grid), dim3(kh.threads), args, (size_t)kh.smem,
+  CK(cudaLaunchKernel(kh.pick(red || mode == MODE_CFL, s, comp), dim3(grid), dim3(kh.threads), args, (size_t)kh.smem,
                       g.stream));
   ++g.launches;
   return 0;
@@ -511,7 +512,8 @@ static int box_launch(pcgb_box* b, int mode) {
     ++g.launches;
     return 0;
   }
-  const int rc = launch(b->ddev, 1, b->tiles, nullptr, mode, b->kh, b->tiles, box_needs_red(b, mode));
+  const int rc = launch(b->ddev, 1, b->tiles, nullptr, mode, b->kh, b->tiles, box_needs_red(b, mode),
+                        (int)(b->nsub % 3), b->hdev.comp != 0);
   if (mode == MODE_SUBSTEP && b->nsub % 3 == 0) b->diag_pending = false;
   return rc;
 }
@@ -530,6 +532,8 @@ static int box_check_state(pcgb_box* b) {
   CK(cudaMemcpyAsync(&st, b->dstate, sizeof(st), cudaMemcpyDeviceToHost, g.stream));
   CK(cudaStreamSynchronize(g.stream));
   if (st.err & PCGB_ERR_TIMEOUT) return set_err(PCGB_E_TIMEOUT, "a bounded device wait gave up (flags %d)", st.err);
+  if (st.err & PCGB_ERR_VARIANT)
+    return set_err(PCGB_E_DEVICE, "a kernel variant for another substep or state mode ran on the box (flags %d)", st.err);
   if (st.err) return set_err(PCGB_E_DEVICE, "device reported error flags %d (non-finite dt or state)", st.err);
   return 0;
 }
@@ -830,6 +834,7 @@ struct pcgb_batch {
   KernelHandle kh;
   bool any_current = false;
   bool red0 = false;   // some box reduces on every substep 1 (lagged CFL dt or periodic diagnostics)
+  bool all_comp = true;   // every box holds the compensated FP32 state
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;
 };
@@ -865,6 +870,7 @@ extern "C" pcgb_batch* pcgb_batch_create(pcgb_box** boxes, int n, int persistent
     t0 += h[i].tiles;
     if (B->boxes[i]->hdev.dt_mode == PCGB_DT_CURRENT) B->any_current = true;
     if (B->boxes[i]->hdev.dt_mode == PCGB_DT_LAGGED || B->boxes[i]->hdev.diag_every > 0) B->red0 = true;
+    if (B->boxes[i]->hdev.comp == 0) B->all_comp = false;
   }
   B->total_tiles = t0;
   B->kh = boxes[0]->kh;
@@ -904,7 +910,7 @@ static int batch_substep(pcgb_batch* B, int s) {
       (rc = launch(B->ddev, (int)B->boxes.size(), B->total_tiles, ctr, MODE_CFL, B->kh, B->grid, true)))
     return rc;
   const bool red = (s == 0) && (B->red0 || batch_diag_pending(B));
-  rc = launch(B->ddev, (int)B->boxes.size(), B->total_tiles, ctr, MODE_SUBSTEP, B->kh, B->grid, red);
+  rc = launch(B->ddev, (int)B->boxes.size(), B->total_tiles, ctr, MODE_SUBSTEP, B->kh, B->grid, red, s, B->all_comp);
   if (s == 0)
     for (auto* b : B->boxes) b->diag_pending = false;
   return rc;
