@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
     const int inb = (int)(nsub & 1ull);
     const CUtensorMap* tmap = &B.tmap[inb];
     const double dt = __ldcg(&S->dt);
-    const bool mode_cfl = (args.mode == MODE_CFL);
+    const bool mode_cfl = KIND == 0 && args.mode == MODE_CFL;   // specialised kernels run substeps only
     const unsigned long long step = nsub / 3ull + __ldcg(&S->step0);
     StepFlags<T> fl;
     fl.s = s;

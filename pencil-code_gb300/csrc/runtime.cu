@@ -299,14 +299,14 @@ static int default_zdepth(const pcgb_box* b) {
 }
 
 // FP32: packed pairs on (32,12) tiles, one 12-warp CTA per SM (on (32,8)
-// tiles, 8 warps, with upwinding or entropy), when a box has at least a wave
+// tiles, 8 warps, with upwinding), when a box has at least a wave
 // of (32,8) column tiles, else on (16,8) tiles with two CTAs per SM (more,
 // smaller work items for small boxes); double-float: packed
 // pairs on (16,12) tiles, one 6-warp CTA per SM; FP64: one 6-warp CTA per SM,
 // (32,6) with 7 fields, (24,8) with 8 (an 8-field ring of (32,6) planes needs
 // 246 KB of shared memory)
 static int default_tile(int tb, int nf, int dfl, int nx, int ny, bool upw) {
-  if (tb == 4) return ((long long)((nx + 31) / 32) * ((ny + 7) / 8) >= 152) ? ((upw || nf == 8) ? 5 : 7) : 6;
+  if (tb == 4) return ((long long)((nx + 31) / 32) * ((ny + 7) / 8) >= 152) ? (upw ? 5 : 7) : 6;
   return dfl ? 5 : (nf == 8 ? 2 : 3);
 }
 
