@@ -45,7 +45,7 @@ inline TileShape tile_shape(int dtype_bytes, int tile, int dfl = 0) {
 struct KernelHandle {
   const void* fn = nullptr;        // with CFL / diagnostic reductions
   const void* fn_nored = nullptr;  // without (same shared memory and block)
-  const void* fn_comp[3] = {nullptr, nullptr, nullptr};   // reduction-free, compensated, substep s (tiles 5, 7)
+  const void* fn_comp[3] = {nullptr, nullptr, nullptr};   // reduction-free, compensated, substep s (FP32 tiles 5-7)
   int smem = 0;
   int threads = 0;
   // the kernel for a launch; s (0..2) and comp describe every box of the launch, s < 0 if they differ
@@ -141,7 +141,7 @@ static KernelHandle make_kernel_handle() {
           case 3: cache[3] = make_kernel_handle<ScalarCell<T, NF, 64, 4>, 64, 4, 9, 1>(); break;   \
           case 4: cache[4] = make_kernel_handle<PairCell<NF, 32, 4>, 32, 4, 8, 2>(); break;        \
           case 5: cache[5] = make_kernel_handle<PairCellTM<NF, 32, 8>, 32, 8, 9, 1, true>(); break; \
-          case 6: cache[6] = make_kernel_handle<PairCell<NF, 16, 8>, 16, 8, 8, 2>(); break;        \
+          case 6: cache[6] = make_kernel_handle<PairCell<NF, 16, 8>, 16, 8, 8, 2, true>(); break;  \
           default: cache[7] = make_kernel_handle<PairCellTM<NF, 32, 12>, 32, 12, 9, 1, true>(); break; \
         }                                                                                          \
       } else {                                                                                     \
@@ -176,7 +176,7 @@ static KernelHandle make_kernel_handle() {
       if constexpr (sizeof(T) == 4) {                                                              \
         switch (tile) {                                                                            \
           case 1: cache[1] = make_kernel_handle<ScalarCell<T, NF, 32, 8, true>, 32, 8, 9, 1>(); break; \
-          case 5: cache[5] = make_kernel_handle<PairCell<NF, 32, 8, true>, 32, 8, 9, 1>(); break;  \
+          case 5: cache[5] = make_kernel_handle<PairCell<NF, 32, 8, true>, 32, 8, 9, 1, true>(); break; \
           default: cache[6] = make_kernel_handle<PairCell<NF, 16, 8, true>, 16, 8, 8, 2>(); break; \
         }                                                                                          \
       } else {                                                                                     \
