@@ -550,8 +550,8 @@ def ensemble_measure(pc, torch, stream, boxes_n: int, steps: int, warmup: int, g
     L = pc.load()
     specs = ens.make_ensemble(boxes_n, seed=seed)
     cells = sum(p.nx * p.ny * p.nz for p, _ in specs)
-    kw = dict(tiles=(5, 6, 7), zdepths=(32, 64), per_size_zdepths=(16, 32, 64, 128), sample=12,
-              per_size_sample=4) if quick else {}
+    kw = dict(tiles=(5, 6, 7), zdepths=(32, 64), per_size_zdepths=(8, 16, 32, 64, 128), sample=12,
+              per_size_sample=8) if quick else {}
     t_tile, t_zd, table = ens.autotune_batch(specs, **kw)
     tuned = ens.with_tiling(specs, t_tile, t_zd)
     out = {}

@@ -90,7 +90,7 @@ def _time_batch(specs, tile, zd_of, steps):
 
 
 def autotune_batch(specs, tiles=(4, 5, 6, 7), zdepths=(16, 32, 64), steps: int = 3, sample: int = 24,
-                   per_size_zdepths=(8, 16, 32, 64, 128), per_size_sample: int = 6):
+                   per_size_zdepths=(8, 16, 32, 64, 128), per_size_sample: int = 8):
     """Pick the tile variant of the batched launch and the z-sweep depth of every box size.
 
     Stage 1 times the tile variants (with one z-depth for all boxes) on a sample of the
