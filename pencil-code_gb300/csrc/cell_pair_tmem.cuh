@@ -122,7 +122,13 @@ struct PairCellTM {
       const St st{pl, this->F};
       const Fac<float>& F = this->F;
       const Phys<float>& P = this->P;
-      const long long cidx = (long long)(z + 3) * this->ps + (long long)(y + 3) * this->px + this->xoff + x;
+      // element offsets in 32 bits (the host keeps 2 fs + 8 ps below 2^32 for these tiles): slice p
+      // of an array at base[p >> 1] + (p & 1) fs + offset, one wide multiply-add per access
+      const uint32_t fs32 = (uint32_t)this->fs, ps32 = (uint32_t)this->ps;
+      const uint32_t ci = (uint32_t)(z + 3) * ps32 + (uint32_t)((y + 3) * this->px + this->xoff + x);
+      float2* const db[2] = {this->dfp, this->dfp + 2 * this->fs};
+      float2* const fb[2] = {this->fout, this->fout + 2 * this->fs};
+      auto at = [&](float2* const* b, int pp, uint32_t o) { return b[pp >> 1] + (uint32_t)((pp & 1) * fs32 + o); };
       float2 cL[4], aL[3][4];   // the leading plane z+3 (aL[0], aL[1]: compact layout only)
       if constexpr (!kCompact) {
         if (z == zfirst) {   // prologue of the tile: planes z-3..z+2 into their slots
@@ -169,11 +175,11 @@ struct PairCellTM {
       for (int p = 0; p < 4; ++p) dfo2[p] = this->dfnext[p];
       if (fl.read_df && active && z + 1 < z1) {
 #pragma unroll
-        for (int p = 0; p < 4; ++p) this->dfnext[p] = this->dfp[p * this->fs + cidx + this->ps];
+        for (int p = 0; p < 4; ++p) this->dfnext[p] = *at(db, p, ci + ps32);
       }
       if (fl.read_df && active && z + kDfPrefetch < z1) {
 #pragma unroll
-        for (int p = 0; p < 4; ++p) prefetch_l2(this->dfp + p * this->fs + cidx + kDfPrefetch * this->ps);
+        for (int p = 0; p < 4; ++p) prefetch_l2(at(db, p, ci + kDfPrefetch * ps32));
       }
       tm_wait_ld();
       tm_tie8(ra1p); tm_tie8(ra1m); tm_tie8(ra2p); tm_tie8(ra2m);
@@ -316,10 +322,10 @@ struct PairCellTM {
       if (active) {
         if (fl.write_df) {
 #pragma unroll
-          for (int p = 0; p < 4; ++p) this->dfp[p * this->fs + cidx] = dsto[p];
+          for (int p = 0; p < 4; ++p) *at(db, p, ci) = dsto[p];
         }
 #pragma unroll
-        for (int p = 0; p < 4; ++p) this->fout[p * this->fs + cidx] = fnew[p];
+        for (int p = 0; p < 4; ++p) *at(fb, p, ci) = fnew[p];
         const bool edge = (x < 3) | (x >= this->nx - 3) | (y < 3) | (y >= this->ny - 3) | (z < 3) | (z >= this->nz - 3);
         if (edge) {
           const Images ix(x, this->nx), iy(y, this->ny), iz(z, this->nz);

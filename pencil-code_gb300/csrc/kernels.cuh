@@ -79,6 +79,14 @@ inline bool upw_tile(int dtype_bytes, int tile, int dfl = 0) {
   return tile == 1 || tile == 2 || tile == 3;
 }
 
+// The tensor-memory cell (FP32 pair tiles 5 and 7 without upwinding) addresses the
+// arrays with 32-bit element offsets of up to 2 fs + 8 ps (fs, ps: elements per slice
+// and per plane).
+inline bool tile_uses_offsets32(int dtype_bytes, int tile, bool upw) {
+  return dtype_bytes == 4 && !upw && (tile == 5 || tile == 7);
+}
+inline bool offsets32_fit(long long fs, long long ps) { return 2 * fs + 8 * ps < (1LL << 32); }
+
 // dfl: FP64-class state held as double-float pairs (8-byte elements, same tiles as FP64)
 // upw: the variant with the upwind corrections
 inline KernelHandle get_kernel(int dtype_bytes, int nf, int tile, int dfl = 0, bool upw = false) {

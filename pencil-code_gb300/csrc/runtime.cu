@@ -305,13 +305,18 @@ static int default_zdepth(const pcgb_box* b) {
 // pairs on (16,12) tiles, one 6-warp CTA per SM; FP64: one 6-warp CTA per SM,
 // (32,6) with 7 fields, (24,8) with 8 (an 8-field ring of (32,6) planes needs
 // 246 KB of shared memory)
-static int default_tile(int tb, int nf, int dfl, int nx, int ny, bool upw) {
-  if (tb == 4) return ((long long)((nx + 31) / 32) * ((ny + 7) / 8) >= 152) ? (upw ? 5 : 7) : 6;
+static int default_tile(int tb, int nf, int dfl, int nx, int ny, int nz, bool upw) {
+  if (tb == 4) {
+    if ((long long)((nx + 31) / 32) * ((ny + 7) / 8) < 152) return 6;
+    if (upw) return 5;
+    const long long px = 16 + (nx + 8 + 15) / 16 * 16, ps = px * (ny + 6);   // the FP32 pair layout
+    return offsets32_fit(ps * (nz + 6), ps) ? 7 : 6;
+  }
   return dfl ? 5 : (nf == 8 ? 2 : 3);
 }
 
 static int set_tiling(pcgb_box* b, int tile, int zd) {
-  if (tile < 0) tile = default_tile(b->tb, b->nf, b->dfl, b->nx, b->ny, b->hdev.lupw != 0);
+  if (tile < 0) tile = default_tile(b->tb, b->nf, b->dfl, b->nx, b->ny, b->nz, b->hdev.lupw != 0);
   if (tile >= num_tiles(b->tb, b->dfl)) return set_err(PCGB_E_ARG, "tile variant %d out of range", tile);
   if ((int)tile_is_pair(b->tb, tile, b->dfl) != b->pairs)
     return set_err(PCGB_E_ARG, "tile %d needs a different device layout than this box was created with", tile);
@@ -319,6 +324,9 @@ static int set_tiling(pcgb_box* b, int tile, int zd) {
   const bool upw = b->hdev.lupw != 0;
   KernelHandle kh = get_kernel(b->tb, b->nf, tile, b->dfl, upw);
   if (!kh.fn && upw) return set_err(PCGB_E_UNSUPPORTED, "tile %d has no upwinding variant", tile);
+  if (tile_uses_offsets32(b->tb, tile, upw) && !offsets32_fit(b->fs, b->ps))
+    return set_err(PCGB_E_UNSUPPORTED, "tile %d addresses a box with 32-bit offsets; one this large needs tile 4 or 6",
+                   tile);
   if (!kh.fn) return set_err(PCGB_E_ARG, "no kernel for tile %d", tile);
   if (kh.smem > g.max_smem) return set_err(PCGB_E_UNSUPPORTED, "tile %d needs %d B shared memory", tile, kh.smem);
   b->tile = tile; b->tx = ts.tx; b->ty = ts.ty; b->kh = kh;
@@ -384,7 +392,7 @@ extern "C" pcgb_box* pcgb_box_create(const pcgb_params* p) {
   b->nx = p->nx; b->ny = p->ny; b->nz = p->nz;
   b->mx = p->nx + 6; b->my = p->ny + 6; b->mz = p->nz + 6;
   {
-    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb, b->nf, b->dfl, p->nx, p->ny, p->lupw_uu || p->lupw_lnrho);
+    const int t0 = p->tile >= 0 ? p->tile : default_tile(b->tb, b->nf, b->dfl, p->nx, p->ny, p->nz, p->lupw_uu || p->lupw_lnrho);
     b->pairs = (t0 < num_tiles(b->tb, b->dfl) && tile_is_pair(b->tb, t0, b->dfl)) ? 1 : 0;
   }
   b->eb = b->pairs ? (b->dfl ? 16 : 8) : b->tb;
@@ -446,7 +454,7 @@ extern "C" size_t pcgb_params_bytes(const pcgb_params* p) {
   if (!p || p->nx < 1 || p->ny < 1 || p->nz < 1 || (p->precision != 4 && p->precision != 8)) return 0;
   const int tb = p->precision, nf = p->lentropy ? 8 : 7;
   const int dfl = (tb == 8 && p->dfloat) ? 1 : 0;
-  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb, nf, dfl, p->nx, p->ny, p->lupw_uu || p->lupw_lnrho);
+  const int t0 = p->tile >= 0 ? p->tile : default_tile(tb, nf, dfl, p->nx, p->ny, p->nz, p->lupw_uu || p->lupw_lnrho);
   const int pairs = (t0 < num_tiles(tb, dfl) && tile_is_pair(tb, t0, dfl)) ? 1 : 0;
   const int eb = pairs ? (dfl ? 16 : 8) : tb, ns = pairs ? 4 : nf;
   const int xoff = 128 / eb;
