@@ -451,7 +451,15 @@ def run_fp64_class(args, pc, torch, stream, peak, peak_kind) -> dict:
                        "peak_kind": peak_kind, "bytes_per_cell_substep": bytes_per_cell_substep(nf, 8)},
                "gpu_launches": launches}
         if name in pipes:
-            rec["compute"] = pipes[name]
+            rec["compute"] = dict(pipes[name])
+            ops = pipes[name].get("fp32_lane_ops_per_cell")
+            if ops:   # compute roofline: FP32 lane operations against 128 FP32 lanes per SM at 2070 MHz
+                nsm = torch.cuda.get_device_properties(0).multi_processor_count
+                peak_ops = nsm * 128 * 2070e6
+                rec["compute"].update({"achieved_fp32_lane_ops_per_s": ops * rate * 1e9,
+                                       "peak_fp32_lane_ops_per_s": peak_ops,
+                                       "frac_of_fp32_peak": ops * rate * 1e9 / peak_ops,
+                                       "peak_basis": f"{nsm} SMs x 128 FP32 lanes x 2070 MHz (the SM clock under load)"})
         out[name] = rec
         torch.cuda.empty_cache()
     return out
