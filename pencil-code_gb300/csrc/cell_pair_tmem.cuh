@@ -28,6 +28,12 @@
 //    after this step's loads have completed.
 // With 12 warps (168 registers) the SM issues from three warps per scheduler
 // instead of two.
+//
+// UPW: the variant with the upwind corrections (lupw_uu, lupw_lnrho; the z part
+// of each 6th difference from the tensor-memory centres, the x and y parts from
+// shared memory, in St::del6u's arithmetic) and with the random helical force
+// added in the last substep's update, as PairCell does it (the reference's
+// timing-run physics).
 #pragma once
 
 #include "cell_pair.cuh"
@@ -58,9 +64,9 @@ __device__ __forceinline__ void tm_tie8(uint32_t r[8]) {
 }
 __device__ __forceinline__ float2 u2f2(uint32_t a, uint32_t b) { return make_float2(__uint_as_float(a), __uint_as_float(b)); }
 
-template <int NF, int TX, int TY>
+template <int NF, int TX, int TY, bool UPW = false>
 struct PairCellTM {
-  using Base = PairCell<NF, TX, TY, false>;
+  using Base = PairCell<NF, TX, TY, UPW>;
   using T = float;
   using Elem = float2;
   static constexpr int NSLICE = 4;
@@ -125,6 +131,14 @@ struct PairCellTM {
       // element offsets in 32 bits (the host keeps 2 fs + 8 ps below 2^32 for these tiles): slice p
       // of an array at base[p >> 1] + (p & 1) fs + offset, one wide multiply-add per access
       const uint32_t fs32 = (uint32_t)this->fs, ps32 = (uint32_t)this->ps;
+      float hzr = 0.f, hzi = 0.f;   // helical fz of this plane, loaded ahead of its use at the update
+      if constexpr (UPW) {
+        if (this->htab != nullptr && fl.s == 2) {
+          const float* fz = this->htab + 8 + 2 * this->nx + 2 * this->ny;
+          hzr = fz[2 * z];
+          hzi = fz[2 * z + 1];
+        }
+      }
       const uint32_t ci = (uint32_t)(z + 3) * ps32 + (uint32_t)((y + 3) * this->px + this->xoff + x);
       float2* const db[2] = {this->dfp, this->dfp + 2 * this->fs};
       float2* const fb[2] = {this->fout, this->fout + 2 * this->fs};
@@ -270,6 +284,23 @@ struct PairCellTM {
       } else {
         c.del2lnrho = c.del2ss = 0.f;
       }
+      if constexpr (UPW) {   // calc_del6_for_upwind, sub.f90:7491-7539
+        auto del6z = [&](int p) {   // der6_main upwind=T along z (deriv.f90:936-1010)
+          const float2 s1 = p_add(cz[4][p], cz[2][p]), s2 = p_add(cz[5][p], cz[1][p]), s3 = p_add(cz[6][p], cz[0][p]);
+          float2 t = p_mul(p_splat(-20.f), cz[3][p]);
+          t = p_fma(p_splat(15.f), s1, t);
+          t = p_fma(p_splat(-6.f), s2, t);
+          return p_mul(p_splat(F.fz), p_add(t, s3));
+        };
+        auto upwind = [&](int p) {
+          return (fabsf(c.uu[0]) * st.del6u(p, 0).x + fabsf(c.uu[1]) * st.del6u(p, 1).x) + fabsf(c.uu[2]) * del6z(p).x;
+        };
+        if (this->upw & UPW_UU) {
+#pragma unroll
+          for (int p = 0; p < 3; ++p) c.upw_u[p] = upwind(p);
+        }
+        if (this->upw & UPW_LNRHO) c.upw_lnrho = upwind(3);
+      }
       float fc[3] = {0.f, 0.f, 0.f};
       if (this->forcing) {   // forcing_cont 'ABC', forcing.f90:5894-5896
         fc[0] = P.fact * (P.abc_c * this->fsz + (P.fact2 * P.abc_b) * this->fcy);
@@ -285,7 +316,7 @@ struct PairCellTM {
       float dt1_l = 0.f;
       if (fl.want_diag) acc_l.reset();
       cell_rhs<float, NF>(c, P, F, fc, this->forcing, this->iso, this->vheat, this->oheat, dfo, fl.alpha, dfn,
-                          fl.want_cfl, fl.want_diag, acc_l, dt1_l, 0);
+                          fl.want_cfl, fl.want_diag, acc_l, dt1_l, UPW ? this->upw : 0);
       if (active) {
         if (fl.want_diag) {
 #pragma unroll
@@ -319,6 +350,18 @@ struct PairCellTM {
         }
       }
       if (!ENTROPY) { fnew[3].y = 0.f; dsto[3].y = 0.f; }
+      if constexpr (UPW) {
+        if (this->htab != nullptr && fl.s == 2) {   // forcing_hel after the step (addforce, forcing.f90:1307)
+          const float qr = rsub(rmul(this->hpr, hzr), rmul(this->hpi, hzi));
+          const float qi = radd(rmul(this->hpr, hzi), rmul(this->hpi, hzr));
+#pragma unroll
+          for (int p = 0; p < 3; ++p) {
+            const float fh = rsub(rmul(this->hc1[p], qr), rmul(this->hc2[p], qi));
+            if (this->htarget) fnew[p].y = __fadd_rn(fnew[p].y, fh);
+            else fnew[p].x = __fadd_rn(fnew[p].x, fh);
+          }
+        }
+      }
       if (active) {
         if (fl.write_df) {
 #pragma unroll

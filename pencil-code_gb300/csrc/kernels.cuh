@@ -13,8 +13,8 @@ namespace pcgb {
 // cell); for FP32 and double-float, ids 4..7 use the packed field-pair layout
 // (cell_pair.cuh: float2 elements; cell_ddpair.cuh: 16-byte dd2 elements).  The
 // FP32 pair tiles 5 (8 warps) and 7 (12 warps, the default for large boxes)
-// keep their z-direction data in tensor memory (cell_pair_tmem.cuh); the
-// upwinding variant of tile 5 is the shared-memory PairCell, tile 7 has none.
+// keep their z-direction data in tensor memory (cell_pair_tmem.cuh), as does
+// the upwinding variant of tile 5; tile 7 has no upwinding variant.
 //   FP32: 0 (32,4)x2  1 (32,8)  2 (16,8)x2  3 (64,4)  4 pair(32,4)x2  5 pair(32,8)  6 pair(16,8)x2  7 pair(32,12)
 //   FP64: 0 (32,4)  1 (16,8)  2 (24,8)  3 (32,6)
 //   double-float: 0..3 as FP64, 4 pair(24,8)  5 pair(16,12)  6 pair(16,8)  7 pair(32,4)
@@ -79,11 +79,10 @@ inline bool upw_tile(int dtype_bytes, int tile, int dfl = 0) {
   return tile == 1 || tile == 2 || tile == 3;
 }
 
-// The tensor-memory cell (FP32 pair tiles 5 and 7 without upwinding) addresses the
-// arrays with 32-bit element offsets of up to 2 fs + 8 ps (fs, ps: elements per slice
-// and per plane).
-inline bool tile_uses_offsets32(int dtype_bytes, int tile, bool upw) {
-  return dtype_bytes == 4 && !upw && (tile == 5 || tile == 7);
+// The tensor-memory cell (FP32 pair tiles 5 and 7) addresses the arrays with 32-bit
+// element offsets of up to 2 fs + 8 ps (fs, ps: elements per slice and per plane).
+inline bool tile_uses_offsets32(int dtype_bytes, int tile) {
+  return dtype_bytes == 4 && (tile == 5 || tile == 7);
 }
 inline bool offsets32_fit(long long fs, long long ps) { return 2 * fs + 8 * ps < (1LL << 32); }
 
@@ -184,7 +183,7 @@ static KernelHandle make_kernel_handle() {
       if constexpr (sizeof(T) == 4) {                                                              \
         switch (tile) {                                                                            \
           case 1: cache[1] = make_kernel_handle<ScalarCell<T, NF, 32, 8, true>, 32, 8, 9, 1>(); break; \
-          case 5: cache[5] = make_kernel_handle<PairCell<NF, 32, 8, true>, 32, 8, 9, 1, true>(); break; \
+          case 5: cache[5] = make_kernel_handle<PairCellTM<NF, 32, 8, true>, 32, 8, 9, 1, true>(); break; \
           default: cache[6] = make_kernel_handle<PairCell<NF, 16, 8, true>, 16, 8, 8, 2>(); break; \
         }                                                                                          \
       } else {                                                                                     \

@@ -308,9 +308,9 @@ static int default_zdepth(const pcgb_box* b) {
 static int default_tile(int tb, int nf, int dfl, int nx, int ny, int nz, bool upw) {
   if (tb == 4) {
     if ((long long)((nx + 31) / 32) * ((ny + 7) / 8) < 152) return 6;
-    if (upw) return 5;
     const long long px = 16 + (nx + 8 + 15) / 16 * 16, ps = px * (ny + 6);   // the FP32 pair layout
-    return offsets32_fit(ps * (nz + 6), ps) ? 7 : 6;
+    if (!offsets32_fit(ps * (nz + 6), ps)) return 6;
+    return upw ? 5 : 7;
   }
   return dfl ? 5 : (nf == 8 ? 2 : 3);
 }
@@ -324,7 +324,7 @@ static int set_tiling(pcgb_box* b, int tile, int zd) {
   const bool upw = b->hdev.lupw != 0;
   KernelHandle kh = get_kernel(b->tb, b->nf, tile, b->dfl, upw);
   if (!kh.fn && upw) return set_err(PCGB_E_UNSUPPORTED, "tile %d has no upwinding variant", tile);
-  if (tile_uses_offsets32(b->tb, tile, upw) && !offsets32_fit(b->fs, b->ps))
+  if (tile_uses_offsets32(b->tb, tile) && !offsets32_fit(b->fs, b->ps))
     return set_err(PCGB_E_UNSUPPORTED, "tile %d addresses a box with 32-bit offsets; one this large needs tile 4 or 6",
                    tile);
   if (!kh.fn) return set_err(PCGB_E_ARG, "no kernel for tile %d", tile);
