@@ -20,7 +20,7 @@ namespace pcgb {
 
 namespace {
 
-constexpr int kTX = 32, kTY = 8, kZC = 32;   // block (x, y) and z-chunk
+constexpr int kTX = 32, kTY = 8, kZC = 64;   // block (x, y) and z-chunk
 constexpr int kThreads = kTX * kTY;
 constexpr int kPF = 4;   // the column's lines are requested into L2 this many planes ahead
 
@@ -34,7 +34,7 @@ __device__ __forceinline__ float der1(float m3, float m2, float m1, float p1, fl
 __device__ __forceinline__ float nanmax(float a, float b) { return (b > a || b != b) ? b : a; }
 
 template <int NF>
-__global__ void __launch_bounds__(kThreads, 3) cfl_pair_kernel(const PcgbBoxDev* __restrict__ Bp, double* partial,
+__global__ void __launch_bounds__(kThreads, 4) cfl_pair_kernel(const PcgbBoxDev* __restrict__ Bp, double* partial,
                                                              unsigned int* done) {
   const PcgbBoxDev& B = *Bp;
   PcgbBoxState* const S = B.state;
