@@ -295,7 +295,11 @@ size_t pcgb_params_bytes(const pcgb_params* p);
 int pcgb_box_info(const pcgb_box* b, int* info, int ninfo);
 
 /* A batch advances many boxes of one class (precision, field count, tile)
-   in one persistent launch per substep. */
+   in one persistent launch per substep.  Each box's result is bitwise the one
+   it has stepped alone when the boxes also agree in the FP32 compensated mode
+   (comp): a batch mixing comp and plain FP32 boxes runs the kernel with the
+   mode read at run time, which can differ from the single-box kernels in the
+   last bits. */
 pcgb_batch* pcgb_batch_create(pcgb_box** boxes, int n, int persistent);
 void pcgb_batch_destroy(pcgb_batch* b);
 /* nsteps RK3 steps for every box; use_graph != 0 captures the substep loop

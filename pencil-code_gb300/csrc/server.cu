@@ -112,7 +112,10 @@ void pcgb_server::finish_box(Req* r, bool ok) {
 
 static int class_key(const Req* r) {
   const int upw = (r->p.lupw_uu || r->p.lupw_lnrho) ? 1 : 0;   // the upwinding kernel variant is its own class
-  return ((upw * 2 + r->p.dfloat) * 16 + r->p.precision) * 16 + (r->p.lentropy ? 8 : 7);
+  // the compensated FP32 state runs kernels compiled per substep, the plain one does not:
+  // separate classes keep every request's result bitwise the one it has alone
+  const int comp = (r->p.precision == 4 && r->p.comp) ? 1 : 0;
+  return (((upw * 2 + comp) * 2 + r->p.dfloat) * 16 + r->p.precision) * 16 + (r->p.lentropy ? 8 : 7);
 }
 
 static long long box_tiles(pcgb_box* b) {
