@@ -55,6 +55,28 @@ def test_mix_equals_alone(pc):
         assert np.array_equal(f, ref), (n, prec, ent)
 
 
+def test_compensated_and_plain_fp32_in_the_mix(pc):
+    """FP32 requests with and without the compensated state (each its own class: the
+    compensated one runs kernels compiled per substep) served together: every result
+    equals the box alone, bitwise."""
+    serve = importlib.import_module("pencil-code_gb300.serve")
+    ens = importlib.import_module("pencil-code_gb300.ensemble")
+    specs = [(32, 31, 2e-3, 1.0, 6, 1), (32, 32, 3e-3, 2.0, 6, 0), (24, 33, 5e-3, 1.0, 5, 0), (40, 34, 2e-3, 3.0, 4, 1)]
+    srv = serve.Server(budget_bytes=20e9, round_steps=2)
+    outs, ids = [], []
+    for n, seed, nu, k, steps, comp in specs:
+        p = _req(pc, n, 4, False, seed, nu, k).update(comp=comp)
+        f = np.zeros(pc.host_shape(p), order="F")
+        outs.append(f)
+        ids.append(srv.submit(p, steps, seed, noise=1e-5, f_out=f))
+    assert srv.drain(600)
+    assert all(srv.poll(i)[0] == 1 for i in ids)
+    srv.close()
+    for (n, seed, nu, k, steps, comp), f in zip(specs, outs):
+        ref = _alone(pc, ens, _req(pc, n, 4, False, seed, nu, k).update(comp=comp), steps, seed)
+        assert np.array_equal(f, ref), (n, comp)
+
+
 def test_admission_budget_and_fifo(pc):
     serve = importlib.import_module("pencil-code_gb300.serve")
     L = pc.load()
