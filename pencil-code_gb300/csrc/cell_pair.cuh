@@ -175,7 +175,7 @@ struct PairCell {
     }
 
     __device__ __forceinline__ void step(const float2* const pl[7], int x, int y, int z, int z1,
-                                         const StepFlags<float>& fl, Acc& acc, float& dt1max) {
+                                         const StepFlags<float>& fl, AccF& acc, float& dt1max) {
       const St st{pl, F};
       const long long cidx = (long long)(z + 3) * ps + (long long)(y + 3) * px + xoff + x;
       float hzr = 0.f, hzi = 0.f;   // fz of this plane, loaded ahead of its use at the update

@@ -123,7 +123,7 @@ struct PairCellTM {
     }
 
     __device__ __forceinline__ void step(const float2* const pl[7], int x, int y, int z, int z1,
-                                         const StepFlags<float>& fl, Acc& acc, float& dt1max, bool active) {
+                                         const StepFlags<float>& fl, AccF& acc, float& dt1max, bool active) {
       using St = typename Base::St;
       const St st{pl, this->F};
       const Fac<float>& F = this->F;
@@ -312,17 +312,12 @@ struct PairCellTM {
       dfo[0] = dfo2[0].x; dfo[1] = dfo2[1].x; dfo[2] = dfo2[2].x; dfo[ILNRHO] = dfo2[3].x;
       if (ENTROPY) dfo[ISS] = dfo2[3].y;
       dfo[IAX] = dfo2[0].y; dfo[IAX + 1] = dfo2[1].y; dfo[IAX + 2] = dfo2[2].y;
-      Acc acc_l;
+      DiagF dg;   // this cell's diagnostic terms, added to the column's sums only on a live lane
       float dt1_l = 0.f;
-      if (fl.want_diag) acc_l.reset();
       cell_rhs<float, NF>(c, P, F, fc, this->forcing, this->iso, this->vheat, this->oheat, dfo, fl.alpha, dfn,
-                          fl.want_cfl, fl.want_diag, acc_l, dt1_l, UPW ? this->upw : 0);
+                          fl.want_cfl, fl.want_diag, dg, dt1_l, UPW ? this->upw : 0);
       if (active) {
-        if (fl.want_diag) {
-#pragma unroll
-          for (int q = 0; q < PCGB_NSLOT; ++q)
-            acc.v[q] = slot_is_max(q) ? fmax(acc.v[q], acc_l.v[q]) : acc.v[q] + acc_l.v[q];
-        }
+        if (fl.want_diag) dg.add_to(acc);
         dt1max = (dt1_l > dt1max || dt1_l != dt1_l) ? dt1_l : dt1max;
       }
 

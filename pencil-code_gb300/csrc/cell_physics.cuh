@@ -5,6 +5,7 @@
 // diagnostic contributions.
 #pragma once
 
+#include <type_traits>
 #include "mhd_common.cuh"
 
 namespace pcgb {
@@ -25,12 +26,26 @@ struct CellIn {
 // Upwinding flags (bits of PcgbBoxDev::lupw): hydro.f90:3662 lupw_uu, density.f90:2772 lupw_lnrho.
 enum { UPW_UU = 1, UPW_LNRHO = 2 };
 
+// Double-float product and sum of FP32 values (FMA TwoProd, TwoSum).
+__device__ __forceinline__ void two_prod_f(float a, float b, float& h, float& l) {
+  h = __fmul_rn(a, b);
+  l = __fmaf_rn(a, b, -h);
+}
+__device__ __forceinline__ void add_df(float& h, float& l, float xh, float xl) {
+  const float s = __fadd_rn(h, xh), bp = __fsub_rn(s, h);
+  const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bp)), __fsub_rn(xh, bp));
+  h = s;
+  l = __fadd_rn(__fadd_rn(l, xl), e);
+}
+
 // RHS of one cell in the order of calc_all_rhs (equ.f90:1268-1274).
 // dfo: df before the substep (already read); dfn: alpha*dfo + RHS.
-template <typename T, int NF>
+// A: the diagnostic sink -- Acc (FP64 sums), AccF (FP32 cells' double-float sums) or
+// DiagF (one FP32 cell's terms).
+template <typename T, int NF, class A>
 __device__ __forceinline__ void cell_rhs(const CellIn<T>& c, const Phys<T>& P, const Fac<T>& F, const T fc[3],
                                          bool forcing, bool iso, bool vheat, bool oheat, const T dfo[NF], T alpha,
-                                         T dfn[NF], bool want_cfl, bool want_diag, Acc& acc, T& dt1max,
+                                         T dfn[NF], bool want_cfl, bool want_diag, A& acc, T& dt1max,
                                          int upw = 0) {
   constexpr int IUX = 0, ILNRHO = 3, ISS = 4, IAX = NF - 3;
   constexpr bool ENTROPY = (NF == 8);
@@ -160,12 +175,26 @@ __device__ __forceinline__ void cell_rhs(const CellIn<T>& c, const Phys<T>& P, c
   }
   if (want_diag) {
     const T b00 = c.a3xy - c.a2xz, b11 = c.a1yz - c.a3xy, b22 = c.a2xz - c.a1yz;
-    const double divb = (double)((b00 + b11) + b22);
     // <A.B> uses the field before the imposed B_ext is added (p%bbb, magnetic.f90:4356,4451)
     const T bbb0 = c.aij[2][1] - c.aij[1][2], bbb1 = c.aij[0][2] - c.aij[2][0], bbb2 = c.aij[1][0] - c.aij[0][1];
-    const double ab = ((double)c.aa[0] * (double)bbb0 + (double)c.aa[1] * (double)bbb1) +
-                      (double)c.aa[2] * (double)bbb2;
-    acc_diag(acc, (double)u2, (double)b2, (double)c.lnrho, divb, (double)j2, ab);
+    if constexpr (std::is_same<A, Acc>::value) {
+      const double divb = (double)((b00 + b11) + b22);
+      const double ab = ((double)c.aa[0] * (double)bbb0 + (double)c.aa[1] * (double)bbb1) +
+                        (double)c.aa[2] * (double)bbb2;
+      acc_diag(acc, (double)u2, (double)b2, (double)c.lnrho, divb, (double)j2, ab);
+    } else {   // FP32 cell: the terms in FP32, <A.B> exactly as a double-float
+      const float divb = (b00 + b11) + b22;
+      float abh, abl, ph, pl;
+      two_prod_f(c.aa[0], bbb0, abh, abl);
+      two_prod_f(c.aa[1], bbb1, ph, pl);
+      add_df(abh, abl, ph, pl);
+      two_prod_f(c.aa[2], bbb2, ph, pl);
+      add_df(abh, abl, ph, pl);
+      const float rho = expf(c.lnrho);
+      DiagF d{u2, b2, 0.5f * rho * u2, rho, divb * divb, j2, abh, abl};
+      if constexpr (std::is_same<A, DiagF>::value) acc = d;
+      else d.add_to(acc);
+    }
   }
 }
 

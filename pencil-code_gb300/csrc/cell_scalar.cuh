@@ -260,7 +260,7 @@ struct ScalarCell {
     }
 
     __device__ __forceinline__ void step(const T* const pl[7], int x, int y, int z, int z1, const StepFlags<T>& fl,
-                                         Acc& acc, T& dt1max) {
+                                         typename AccOf<T>::type& acc, T& dt1max) {
       const St st{pl, F};
       const long long cidx = (long long)(z + 3) * ps + (long long)(y + 3) * px + xoff + x;
       T dfo[NF];

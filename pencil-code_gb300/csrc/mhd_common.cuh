@@ -79,14 +79,62 @@ __device__ __forceinline__ void make_phys(Phys<T>& P, const PcgbBoxDev& B) {
   P.maxdiffus = T(mdiff);
 }
 
-// Per-thread FP64 reduction accumulators.
+// Per-thread FP64 reduction accumulators (FP64 and double-float cells).
 struct Acc {
   double v[PCGB_NSLOT];
   __device__ __forceinline__ void reset() {
 #pragma unroll
     for (int i = 0; i < PCGB_NSLOT; ++i) v[i] = 0.0;
   }
+  __device__ __forceinline__ double get(int q) const { return v[q]; }
 };
+
+// Per-thread diagnostic accumulators of the FP32 cells as double-float sums on the
+// FP32 pipes: each addend's rounding error is caught exactly (TwoSum) and summed in
+// lo, so a column's sum keeps about 48 bits; the maxima are exact in FP32.  (FP64
+// arithmetic per cell -- an exp and about forty adds, multiplies and conversions --
+// would run at GB300's FP64 rate, 1/64 of FP32's, and took longer than the RHS.)
+struct AccF {
+  float hi[PCGB_NSLOT], lo[PCGB_NSLOT];
+  __device__ __forceinline__ void reset() {
+#pragma unroll
+    for (int i = 0; i < PCGB_NSLOT; ++i) hi[i] = lo[i] = 0.f;
+  }
+  __device__ __forceinline__ void add(int q, float x) {
+    const float s = __fadd_rn(hi[q], x), bp = __fsub_rn(s, hi[q]);
+    const float e = __fadd_rn(__fsub_rn(hi[q], __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    hi[q] = s;
+    lo[q] = __fadd_rn(lo[q], e);
+  }
+  __device__ __forceinline__ void add2(int q, float xh, float xl) {   // a double-float addend
+    add(q, xh);
+    lo[q] = __fadd_rn(lo[q], xl);
+  }
+  __device__ __forceinline__ void max(int q, float x) { hi[q] = fmaxf(hi[q], x); }
+  __device__ __forceinline__ double get(int q) const { return (double)hi[q] + (double)lo[q]; }
+};
+
+// One FP32 cell's diagnostic terms, for cells that add them only when their lane is live.
+struct DiagF {
+  float u2, b2, ekin, rho, divb2, j2, abh, abl;
+  __device__ __forceinline__ void add_to(AccF& a) const {
+    a.add(PCGB_S_U2SUM, u2);
+    a.max(PCGB_S_U2MAX, u2);
+    a.add(PCGB_S_B2SUM, b2);
+    a.max(PCGB_S_B2MAX, b2);
+    a.add(PCGB_S_EKINSUM, ekin);
+    a.add(PCGB_S_RHOSUM, rho);
+    a.add(PCGB_S_DIVB2SUM, divb2);
+    a.add(PCGB_S_J2SUM, j2);
+    a.add2(PCGB_S_ABSUM, abh, abl);
+  }
+};
+
+// Accumulator type of a cell policy: AccF for FP32 arithmetic, Acc otherwise.
+template <typename T>
+struct AccOf { using type = Acc; };
+template <>
+struct AccOf<float> { using type = AccF; };
 
 __device__ __forceinline__ bool slot_is_max(int s) {
   return s == PCGB_S_DT1MAX || s == PCGB_S_U2MAX || s == PCGB_S_B2MAX;

@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
     if constexpr (TMC > 0) { cell.tm = tm_thread; cell.zfirst = z0; }
     const bool warp_live = __any_sync(0xffffffffu, active);
 
-    Acc acc;
+    typename AccOf<T>::type acc;
     acc.reset();
     T dt1max = T(0);
 
@@ -292,10 +292,9 @@ __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs ar
 
     // ---- per-tile reduction (fixed order: lanes, then warps) ----
     if (need_red) {
-      acc.v[PCGB_S_DT1MAX] = (double)dt1max;
 #pragma unroll
       for (int q = 0; q < PCGB_NSLOT; ++q) {
-        double vq = acc.v[q];
+        double vq = (q == PCGB_S_DT1MAX) ? (double)dt1max : acc.get(q);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) vq = red_op(q, vq, __shfl_xor_sync(0xffffffffu, vq, o));
         if (lane == 0) red[warp * PCGB_NSLOT + q] = vq;
