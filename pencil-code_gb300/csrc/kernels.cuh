@@ -46,11 +46,16 @@ struct KernelHandle {
   const void* fn = nullptr;        // with CFL / diagnostic reductions
   const void* fn_nored = nullptr;  // without (same shared memory and block)
   const void* fn_comp[3] = {nullptr, nullptr, nullptr};   // reduction-free, compensated, substep s (FP32 tiles 5-7)
+  const void* fn_comp_red = nullptr;                        // with reductions, compensated, substep 1
   int smem = 0;
   int threads = 0;
-  // the kernel for a launch; s (0..2) and comp describe every box of the launch, s < 0 if they differ
-  const void* pick(bool red, int s = -1, bool comp = false) const {
-    if (!red && comp && s >= 0 && s < 3 && fn_comp[s]) return fn_comp[s];
+  // the kernel for a launch; s (0..2) and comp describe every box of the launch, s < 0 if they
+  // differ; substep: a substep launch (not the CFL pass)
+  const void* pick(bool red, int s = -1, bool comp = false, bool substep = true) const {
+    if (comp && substep && s >= 0 && s < 3) {
+      if (!red && fn_comp[s]) return fn_comp[s];
+      if (red && s == 0 && fn_comp_red) return fn_comp_red;
+    }
     return red ? fn : fn_nored;
   }
 };
@@ -125,7 +130,9 @@ static KernelHandle make_kernel_handle() {
     h.fn_comp[0] = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, false, 1>);
     h.fn_comp[1] = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, false, 2>);
     h.fn_comp[2] = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, false, 3>);
+    h.fn_comp_red = reinterpret_cast<const void*>(&mhd_substep_kernel<CELL, TX, TY, R, MB, true, 1>);
     for (const void* fn : h.fn_comp) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, h.smem);
+    cudaFuncSetAttribute(h.fn_comp_red, cudaFuncAttributeMaxDynamicSharedMemorySize, h.smem);
   }
   return h;
 }

@@ -66,14 +66,15 @@ struct DriverCfg {
 // and 3, and substep 1 with a fixed dt and no diagnostics due): no per-thread
 // FP64 accumulators, no reduction code.  The host picks it; a box that
 // nevertheless finds a reduction due flags PCGB_ERR_NORED.
-// KIND = 1..3: reduction-free and specialised at compile time for substep
-// KIND-1 of boxes in the FP32 compensated mode, so that the substep's branches
-// of the update (df read and written, the carry's form) fold away; the host
-// picks it for such launches, a box in another substep or mode flags
-// PCGB_ERR_VARIANT.  KIND = 0: the substep and mode are read at run time.
+// KIND = 1..3: specialised at compile time for substep KIND-1 of boxes in the
+// FP32 compensated mode, so that the substep's branches of the update (df read
+// and written, the carry's form) fold away -- reduction-free, or with RED for
+// substep 1 (the substep that reduces); the host picks it for such launches, a
+// box in another substep or mode flags PCGB_ERR_VARIANT.  KIND = 0: the substep
+// and mode are read at run time.
 template <class CELL, int TX, int TY, int RING, int MINB, bool RED, int KIND = 0>
 __global__ void __launch_bounds__(TX* TY, MINB) mhd_substep_kernel(LaunchArgs args) {
-  static_assert(KIND == 0 || !RED, "substep-specialised kernels are reduction-free");
+  static_assert(KIND == 0 || !RED || KIND == 1, "reductions happen on substep 1 only");
   using C = DriverCfg<CELL, TX, TY, RING>;
   using T = typename CELL::T;
   using Elem = typename CELL::Elem;

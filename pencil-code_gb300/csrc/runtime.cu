@@ -495,7 +495,8 @@ static int launch(const PcgbBoxDev* dboxes, int nboxes, int total_tiles, unsigne
   a.inject_wait_failure = g.inject_wait_failure;
   if (counter) CK(cudaMemsetAsync(counter, 0, sizeof(unsigned int), g.stream));
   void* args[] = {&a};
-  CK(cudaLaunchKernel(kh.pick(red || mode == MODE_CFL, s, comp), dim3(grid), dim3(kh.threads), args, (size_t)kh.smem,
+  CK(cudaLaunchKernel(kh.pick(red || mode == MODE_CFL, s, comp, mode == MODE_SUBSTEP), dim3(grid), dim3(kh.threads), args,
+                      (size_t)kh.smem,
                       g.stream));
   ++g.launches;
   return 0;
