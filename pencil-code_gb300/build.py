@@ -22,7 +22,7 @@ LIB_SGL = os.path.join(OUT, "libpcgb300_sgl.so")
 SGL_SOURCES = {"runtime.cu": "runtime_sgl.o"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["kernels_f32_7.cu", "kernels_f32_8.cu", "kernels_f64_7.cu", "kernels_f64_8.cu", "kernels_dd_7.cu",
-           "kernels_dd_8.cu", "kernels_upw_f32.cu", "kernels_upw_f64.cu", "kernels_upw_dd.cu", "helical.cu", "cfl_pair.cu", "boundcond.cu",
+           "kernels_dd_8.cu", "kernels_upw_f32.cu", "kernels_upw_f64.cu", "kernels_upw_dd_7.cu", "kernels_upw_dd_8.cu", "helical.cu", "cfl_pair.cu", "boundcond.cu",
            "aux_kernels.cu", "runtime.cu", "noalloc.cu", "server.cu"]
 HEADERS = ["mhd_common.cuh", "mhd_driver.cuh", "cell_physics.cuh", "cell_scalar.cuh", "cell_pair.cuh", "kernels.cuh", "pcgb_box.h", "pcgb_ptx.cuh", "aux_kernels.h", "dd.cuh", "cell_ddpair.cuh", "helical.h", "cfl_pair.h", "boundcond.h", "params_check.h", "cell_pair_tmem.cuh"]
 
