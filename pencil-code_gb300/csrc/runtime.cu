@@ -1085,10 +1085,13 @@ static REAL_PCGB* g_hostf = nullptr;
 
 // The plug-in's host f-array is the Fortran build's REAL (double, or float in
 // the single-precision library).
-static int host_load(pcgb_box* b, const double* f, double t) { return pcgb_box_load(b, f, t); }
+#ifdef PCGB_REAL_SINGLE
 static int host_load(pcgb_box* b, const float* f, double t) { return pcgb_box_load_f32(b, f, t); }
-static int host_store(pcgb_box* b, double* f) { return pcgb_box_store(b, f); }
 static int host_store(pcgb_box* b, float* f) { return pcgb_box_store_f32(b, f); }
+#else
+static int host_load(pcgb_box* b, const double* f, double t) { return pcgb_box_load(b, f, t); }
+static int host_store(pcgb_box* b, double* f) { return pcgb_box_store(b, f); }
+#endif
 
 extern "C" int pcgb_set_params(const pcgb_params* p) {
   if (validate(p)) return g_err;
