@@ -82,9 +82,7 @@ __global__ void helical_tables_kernel(const HelRec* ring, const PcgbBoxState* S,
     tab[threadIdx.x] = r.coef1[threadIdx.x];
     tab[3 + threadIdx.x] = r.coef2[threadIdx.x];
   }
-  double* fx = tab + 8;
-  double* fy = fx + 2 * g.nx;
-  double* fz = fy + 2 * g.ny;
+  double* fx = tab + 8;   // fx [2 nx], then fy [2 ny] and fz [2 nz], consecutive
   // the same tables rounded to float, after the double ones (for FP32 states)
   float* tabf = reinterpret_cast<float*>(tab + hel_tab_doubles(g.nx, g.ny, g.nz));
   if (threadIdx.x < 3) {
