@@ -29,6 +29,7 @@ MODES = {
     "dfloat": dict(precision=8, dfloat=1, tile=3),
     "dfloat_pair": dict(precision=8, dfloat=1, tile=5),
     "f32pair": dict(precision=4, comp=1, tile=6),
+    "f32pair7": dict(precision=4, comp=1, tile=7),   # the 12-warp tensor-memory tile
     "f32": dict(precision=4, comp=1, tile=0),
 }
 
@@ -87,7 +88,7 @@ def test_z_boundaries_match_oracle(pc, ic, orc, mode):
     assert abs(box.time()[0] - t_ref) <= 1e-12 * t_ref
 
 
-@pytest.mark.parametrize("mode", ["f64", "f32pair"])
+@pytest.mark.parametrize("mode", ["f64", "f32pair", "f32pair7"])
 def test_x_and_y_boundaries_edges_and_corners(pc, ic, orc, mode):
     """x and y non-periodic, z periodic: boundconds_x before _y, so the corner
     ghosts are the y condition applied to x-filled rows."""

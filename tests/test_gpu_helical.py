@@ -57,11 +57,12 @@ def _oracle_run(orc, p, f0, kvec, kav, nsteps, ldt=False):
     return f, t
 
 
-@pytest.mark.parametrize("mode", ["f64", "dfloat", "dfloat_pair", "f32pair", "f32"])
+@pytest.mark.parametrize("mode", ["f64", "dfloat", "dfloat_pair", "f32pair", "f32pair7", "f32"])
 def test_helical_forcing_matches_oracle(pc, orc, mode):
     d, kvec, kav = _fixture()
     kw = dict(f64=dict(), dfloat=dict(dfloat=1, tile=0), dfloat_pair=dict(dfloat=1, tile=5),
-              f32pair=dict(precision=4, comp=1, tile=5), f32=dict(precision=4, comp=1, tile=0))[mode]
+              f32pair=dict(precision=4, comp=1, tile=5), f32pair7=dict(precision=4, comp=1, tile=7),
+              f32=dict(precision=4, comp=1, tile=0))[mode]
     p = _params(pc, d, **kw)
     f0 = _initial(pc, p)
     box = pc.Box(p)
