@@ -303,6 +303,10 @@ def run_ours(args):
         p.tile = args.tile
     if args.zdepth > 0:
         p.zdepth = args.zdepth
+    if not timings and args.dt_mode:   # the CFL timestep instead of the fixed dt (1 lagged, 2 current)
+        p.update(dt=0.0, dt_mode=args.dt_mode, cdt=0.4)
+    if not timings and args.diag_every:
+        p.diag_every = args.diag_every
     nf = 8 if args.lentropy else 7
     box = pc.Box(p)
     if timings:
@@ -392,7 +396,10 @@ def run_ours(args):
                                    (f"{'entropy' if args.lentropy else 'isothermal'} MHD {n}^3, {nf} fields, "
                                     f"{'FP32 compensated' if prec == 4 else ('FP64-class double-float' if args.dfloat else 'FP64')}"
                                     f", nu=eta=5e-4, ABC k=2 ampl 0.02, "
-                                    f"dt=2e-4"), "grid": n, "fields": nf,
+                                    + (f"CFL dt cdt=0.4 ({'lagged' if args.dt_mode == 1 else 'current'})"
+                                       if args.dt_mode else "dt=2e-4")
+                                    + (f", diagnostics every {args.diag_every} steps" if args.diag_every else "")),
+                       "grid": n, "fields": nf,
                        "tile": info["tile"], "zdepth": info["zdepth"],
                        "l2": "inputs larger than L2 (state %.1f GB)" % (3 * nf * cells * prec / 1e9),
                        "parallelism": f"replicas x{ws}"},
@@ -674,6 +681,9 @@ def main():
                     help="with --precision 8: double-float state and arithmetic on the FP32 pipes")
     ap.add_argument("--tile", type=int, default=-1)
     ap.add_argument("--zdepth", type=int, default=0)
+    ap.add_argument("--dt-mode", type=int, default=0, choices=[0, 1, 2],
+                    help="headline physics with the CFL dt: 1 lagged by a step (the GPU path's default), 2 current")
+    ap.add_argument("--diag-every", type=int, default=0, help="device diagnostics every N steps")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-class", action="store_true",
