@@ -4,7 +4,7 @@
 // arrival order while their device memory (pcgb_params_bytes) fits the budget
 // and the active count is below max_active, creates and seeds their boxes on
 // the device, and picks the requests to advance: the oldest request and the
-// younger requests of its class (precision, field count, kernel variant) that
+// younger requests of its class (precision, field count, kernel variant and tile) that
 // fit into the kernel waves the oldest one occupies on its own (tiles rounded
 // up to whole waves of the GPU), so batching never lengthens the oldest
 // request's substeps; when that leaves less than one wave of work on the
@@ -115,7 +115,28 @@ static int class_key(const Req* r) {
   // the compensated FP32 state runs kernels compiled per substep, the plain one does not:
   // separate classes keep every request's result bitwise the one it has alone
   const int comp = (r->p.precision == 4 && r->p.comp) ? 1 : 0;
-  return (((upw * 2 + comp) * 2 + r->p.dfloat) * 16 + r->p.precision) * 16 + (r->p.lentropy ? 8 : 7);
+  // a batched launch carries one tile variant
+  return ((((upw * 2 + comp) * 2 + r->p.dfloat) * 16 + r->p.precision) * 16 + (r->p.lentropy ? 8 : 7)) * 8 +
+         r->p.tile;
+}
+
+// Tiling of a request that names none: FP32 pairs on (16,8) tiles with two CTAs per SM
+// for boxes under a wave of (32,8) column tiles, on the 12-warp (32,12) tile above;
+// double-float pairs on the 6-warp (16,12) tile; FP64 field-major (16,8).  z-depth n/4
+// within [16, 64]: short sweeps give small boxes enough tiles, long ones keep the
+// six-plane ring prologue of each tile a small share of a large box's planes.
+static void request_tiling(pcgb_params& p) {
+  if (p.tile < 0) {
+    if (p.precision == 4) {
+      const bool upw = p.lupw_uu || p.lupw_lnrho;
+      const long long px = 16 + (p.nx + 8 + 15) / 16 * 16, ps = px * (p.ny + 6), fs = ps * (p.nz + 6);
+      const bool offsets32 = 2 * fs + 8 * ps < (1LL << 32);   // the 12-warp tile's element offsets
+      p.tile = ((long long)((p.nx + 31) / 32) * ((p.ny + 7) / 8) >= 152 && !upw && offsets32) ? 7 : 6;
+    } else {
+      p.tile = p.dfloat ? 5 : 1;
+    }
+  }
+  if (p.zdepth <= 0) p.zdepth = std::min(64, std::max(16, p.nz / 4));
 }
 
 static long long box_tiles(pcgb_box* b) {
@@ -279,9 +300,7 @@ extern "C" long long pcgb_server_submit(pcgb_server* s, const pcgb_params* p, in
     if (!pcgb::axis_periodic(*p, d)) return -1;   // so do the ghost passes of non-periodic boundaries
   Req* r = new Req();
   r->p = *p;
-  // (16,8) tiles suit small boxes: packed pairs for FP32 and double-float, field-major for FP64
-  if (r->p.tile < 0) r->p.tile = (r->p.precision == 4 || r->p.dfloat) ? 6 : 1;
-  if (r->p.zdepth <= 0) r->p.zdepth = 16;
+  request_tiling(r->p);
   r->nsteps = nsteps;
   r->seed = seed;
   r->noise = noise_ampl;

@@ -19,11 +19,22 @@ def _req(pc, n, prec, ent, seed, nu, k):
     return p
 
 
+def _request_tiling(q):
+    """The server's tiling of a request that names none (request_tiling in csrc/server.cu)."""
+    if q.precision == 4:
+        px = 16 + (q.nx + 8 + 15) // 16 * 16
+        ps = px * (q.ny + 6)
+        big = ((q.nx + 31) // 32) * ((q.ny + 7) // 8) >= 152 and not (q.lupw_uu or q.lupw_lnrho)
+        q.tile = 7 if big and 2 * ps * (q.nz + 6) + 8 * ps < (1 << 32) else 6
+    else:
+        q.tile = 5 if q.dfloat else 1
+    q.zdepth = min(64, max(16, q.nz // 4))
+
+
 def _alone(pc, ens, p, steps, seed):
     q = pc.default_params()
     q.update(**p.as_dict())
-    q.tile = 6 if (q.precision == 4 or q.dfloat) else 1
-    q.zdepth = 16
+    _request_tiling(q)
     b = pc.Box(q)
     ens.init_box(b, q, seed)
     b.steps(steps)
