@@ -310,7 +310,7 @@ int pcgb_batch_steps(pcgb_batch* b, int nsteps, int use_graph, int graph_steps);
    a step count and a seeded initial condition) are admitted in arrival order
    while their device memory fits the budget.  Each round advances the oldest
    request together with the younger requests of its class (precision, field
-   count, kernel variant) that fit into the kernel waves the oldest one fills
+   count, kernel variant, state mode, tile) that fit into the kernel waves the oldest one fills
    alone, and, while less than one wave of the GPU is busy, younger requests of
    other classes: one persistent launch per substep per class, the classes on
    streams of their own, in rounds of at most round_steps RK3 steps.  Boxes that
@@ -323,8 +323,11 @@ pcgb_server* pcgb_server_create(size_t mem_budget_bytes, int max_active, int rou
 /* init: Gaussian noise of amplitude noise_ampl on aa (seeded), ABC flow of
    amplitude abc_ampl on uu when abc_ampl != 0.  f_out, if not NULL, receives
    the final f(mx,my,mz,nf) (double, Fortran order).  Returns a request id >= 0,
-   or -1 for a bad request (requests with lforcing_hel are refused: that forcing
-   runs through the box API). */
+   or -1 for a bad request (requests with lforcing_hel or non-periodic
+   boundaries are refused: those run through the box API).  A request with
+   tile < 0 gets its tiling by size: FP32 on tile 7 from 152 column tiles of
+   (32,8) up (tile 6 below, and with upwinding), double-float on tile 5, FP64
+   on tile 1; zdepth <= 0 becomes nz/4 within [16, 64]. */
 long long pcgb_server_submit(pcgb_server* s, const pcgb_params* p, int nsteps, unsigned long long seed,
                              double noise_ampl, double abc_ampl, double* f_out);
 /* 1 when request id is done (times[0..2] = submitted, started, finished;
